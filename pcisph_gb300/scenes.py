@@ -1,0 +1,141 @@
+"""Deterministic analytic scenes for the PCISPH step.
+
+The reference builds its scenes from ``.xraw`` voxel files
+(PCISPH/src/scenes.cpp:76-149, 217-245). The workloads here are analytic
+instead: jittered fluid lattices in a box with reflecting walls. Every random
+number comes from a counter-based hash of (seed, particle id, axis), so a scene
+is the same on every machine and in every process.
+
+Physics maps onto the reference's parametrisation (Fluid.cpp:377-401) through
+``particle_radius = d / 2``: then h = 4r = 2d and m = rho0 (2r)^3 = rho0 d^3.
+"""
+from dataclasses import dataclass, field
+
+import numpy as np
+
+_M1 = np.uint64(0xBF58476D1CE4E5B9)
+_M2 = np.uint64(0x94D049BB133111EB)
+_GOLD = np.uint64(0x9E3779B97F4A7C15)
+
+
+def _mix64(z):
+    """splitmix64 finaliser (Steele, Lea, Flood 2014), vectorised over uint64."""
+    z = (z ^ (z >> np.uint64(30))) * _M1
+    z = (z ^ (z >> np.uint64(27))) * _M2
+    return z ^ (z >> np.uint64(31))
+
+
+def uniform(seed, ids, axis, stream=0):
+    """U[0,1) per (seed, id, axis, stream); float64 with 53 random bits."""
+    with np.errstate(over="ignore"):
+        ids = np.asarray(ids, np.uint64)
+        base = _mix64(np.uint64(seed) * _GOLD + np.uint64(stream) * np.uint64(0xD1B54A32D192ED03))
+        z = _mix64(base ^ (ids * np.uint64(4) + np.uint64(axis)) * _GOLD)
+    return (z >> np.uint64(11)).astype(np.float64) * (1.0 / 9007199254740992.0)
+
+
+@dataclass
+class Scene:
+    """One scene: initial state plus the physical parameters of the step."""
+    name: str
+    fluid_pos: np.ndarray                  # (N, 3) float32
+    spacing: float                         # lattice spacing d
+    delta_t: float
+    box_lo: tuple = (0.0, 0.0, 0.0)
+    box_hi: tuple = (0.0, 0.0, 0.0)
+    boundary_pos: np.ndarray = field(default_factory=lambda: np.zeros((0, 3), np.float32))
+    fluid_vel: np.ndarray = None           # (N, 3) float32 or None (zero)
+    rest_density: float = 1000.0
+    viscosity: float = 0.2
+    surface_tension: float = 0.5
+    gravity: float = -9.81
+    threshold: float = 0.01
+    min_iters: int = 3
+    max_iters: int = 50
+    walls: bool = True
+    restitution: float = 0.5
+    steps: int = 0                         # the workload's step count
+
+    @property
+    def particle_radius(self):
+        return 0.5 * self.spacing
+
+    @property
+    def fluid_count(self):
+        return int(self.fluid_pos.shape[0])
+
+    @property
+    def boundary_count(self):
+        return int(self.boundary_pos.shape[0])
+
+
+def lattice_block(nx, ny, nz, d, origin, seed, jitter=0.05, id_offset=0):
+    """(nx*ny*nz, 3) float32 lattice, x fastest, points at cell centres plus U(+-jitter*d)."""
+    ix, iy, iz = np.meshgrid(np.arange(nx), np.arange(ny), np.arange(nz), indexing="ij")
+    idx = np.stack([ix.ravel(order="F"), iy.ravel(order="F"), iz.ravel(order="F")], 1).astype(np.float64)
+    n = idx.shape[0]
+    ids = np.arange(n, dtype=np.uint64) + np.uint64(id_offset)
+    pos = (idx + 0.5) * d + np.asarray(origin, np.float64)
+    if jitter:
+        for a in range(3):
+            pos[:, a] += (2.0 * uniform(seed, ids, a) - 1.0) * jitter * d
+    return pos.astype(np.float32)
+
+
+def dam_break(n_side=32, seed=0, extent=0.64, box=(1.6, 1.2, 0.8), delta_t=None, steps=1000, **kw):
+    """Config 0/1 dam break: an n_side^3 jittered lattice filling [0, extent]^3 in a box."""
+    d = extent / n_side
+    if delta_t is None:
+        delta_t = 1e-3 * (d / 0.02)
+    pos = lattice_block(n_side, n_side, n_side, d, (0, 0, 0), seed)
+    return Scene(f"dam_break_{n_side}^3", pos, d, delta_t, (0.0, 0.0, 0.0), tuple(box), steps=steps, **kw)
+
+
+def config0():
+    """32,768 particles, d = 0.02 m, dt = 1e-3 s, 1000 steps."""
+    return dam_break(32, seed=0, delta_t=1e-3, steps=1000)
+
+
+def config1():
+    """1,048,576 particles, d = 0.005 m, dt = 2.5e-4 s, 500 steps (same physical box)."""
+    return dam_break(128, seed=0, delta_t=2.5e-4, steps=500)
+
+
+def config2():
+    """8,388,608 particles: two 256x128x128 blocks (d = 0.0025 m) at opposite ends of
+    [0,1.6]x[0,0.8]x[0,0.4], dt = 1.25e-4 s, 200 steps."""
+    d = 0.0025
+    a = lattice_block(256, 128, 128, d, (0.0, 0.0, 0.0), seed=2)
+    b = lattice_block(256, 128, 128, d, (1.6 - 256 * d, 0.0, 0.0), seed=2, id_offset=256 * 128 * 128)
+    pos = np.concatenate([a, b])
+    return Scene("two_blocks_8M", pos, d, 1.25e-4, (0.0, 0.0, 0.0), (1.6, 0.8, 0.4), steps=200)
+
+
+def small_dam(n_side=16, seed=0, **kw):
+    """A small dam break with config-0 physics for tests (same spacing, fewer particles)."""
+    d = 0.02
+    return dam_break(n_side, seed=seed, extent=n_side * d, delta_t=1e-3, **kw)
+
+
+def boundary_box(lo, hi, d, layers=2):
+    """Boundary particles lining the inside of a box (floor and four side walls), reference style.
+
+    The reference samples boundary voxels into ppd^3 particle lattices
+    (scenes.cpp:88-98, 137-145); this is the analytic counterpart: ``layers``
+    sheets of spacing d below the floor and outside each side wall.
+    """
+    lo, hi = np.asarray(lo, np.float64), np.asarray(hi, np.float64)
+    pts = []
+    nx = int(round((hi[0] - lo[0]) / d)) + 2 * layers
+    ny = int(round((hi[1] - lo[1]) / d)) + layers
+    nz = int(round((hi[2] - lo[2]) / d)) + 2 * layers
+    for k in range(nz):
+        for j in range(ny):
+            for i in range(nx):
+                x = lo[0] + (i - layers + 0.5) * d
+                y = lo[1] + (j - layers + 0.5) * d
+                z = lo[2] + (k - layers + 0.5) * d
+                inside = (lo[0] <= x <= hi[0]) and (lo[2] <= z <= hi[2]) and (y >= lo[1])
+                if not inside:
+                    pts.append((x, y, z))
+    return np.asarray(pts, np.float32).reshape(-1, 3)
