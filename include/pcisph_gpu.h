@@ -1,0 +1,241 @@
+/*
+ * pcisph_gpu.h -- C ABI of the GB300 (sm_103a) PCISPH time step.
+ *
+ * Drop-in for the reference's simulation step, class sim::Fluid
+ * (PCISPH/src/sim/Fluid.h:13-102, Fluid.cpp:32-466), and for the clogs radix
+ * sort it calls (libs/clogs/include/clogs/radixsort.h:55-211). Plain C types
+ * only: pointers, sizes, status codes. All device memory of a context is owned
+ * by the context; callers pass host or device pointers to import and export
+ * state. Calls on one context are not thread-safe; use one context per thread.
+ * Every call returns PCISPH_OK or an error code; pcisph_last_error() gives the
+ * message of the last failing call on the calling thread. Nothing throws
+ * across this boundary and no kernel traps: device-side failures are status
+ * bits read by pcisph_last_stats().
+ *
+ * Host-side C++ mirror: include/pcisph_fluid.hpp (class pcisph::Fluid).
+ */
+#ifndef PCISPH_GPU_H
+#define PCISPH_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PCISPH_ABI_VERSION 1
+
+#if defined(__GNUC__)
+#define PCISPH_API __attribute__((visibility("default")))
+#else
+#define PCISPH_API
+#endif
+
+/* ------------------------------------------------------------ status codes */
+enum pcisph_status {
+    PCISPH_OK = 0,
+    PCISPH_ERR_INVALID_ARG = 1,   /* bad pointer, size, layout or enum value */
+    PCISPH_ERR_OOM = 2,           /* device allocation failed */
+    PCISPH_ERR_CUDA = 3,          /* a CUDA runtime call failed (message has the CUDA error) */
+    PCISPH_ERR_INCONSISTENT = 4,  /* state size does not match the counts (Fluid.cpp:90-106) */
+    PCISPH_ERR_NOT_READY = 5,     /* state not set yet */
+    PCISPH_ERR_TIMEOUT = 6        /* a bounded device wait gave up */
+};
+
+/* Step status bits, written on the device, read through pcisph_last_stats(). */
+enum pcisph_step_status {
+    PCISPH_STEP_NOT_CONVERGED = 1u, /* max iterations reached with max error >= threshold */
+    PCISPH_STEP_NONFINITE = 2u,     /* a predicted density was NaN or infinite */
+    PCISPH_STEP_BAD_INDEX = 4u      /* a sorted key or source index was out of range (reorder skipped it) */
+};
+
+/* --------------------------------------------------------------- params */
+/* Mirror of Simulation_Params (PCISPH/data/kernels/Simulation_Params.h:18-44): 20 x 4 B, packed. */
+typedef struct pcisph_sim_params {
+    float particle_radius;
+    float particle_mass;
+    float rest_density;
+    uint32_t boundary_count;
+    uint32_t fluid_count;
+    float kernel_radius;
+    float kernel_radius2;
+    uint32_t bucket_count;
+    float cell_size;
+    float poly6_normalization;
+    float poly6_d1_normalization;
+    float viscosity_d2_normalization;
+    float spiky_d1_normalization;
+    float surface_tension_coefficient;
+    float surface_tension_term;
+    float surface_tension_normalization;
+    float viscosity_constant;
+    float gravity;
+    float delta_t;
+    float density_variation_scaling_factor;
+} pcisph_sim_params;
+
+/* Step options. The reference fixes these in code; defaults reproduce it. */
+typedef struct pcisph_options {
+    int32_t min_iterations;        /* default 3: the reference tests convergence from i >= 2 (Fluid.cpp:250, :284) */
+    int32_t max_iterations;        /* default 7 (Fluid.cpp:251) */
+    int32_t walls;                 /* default 0 (reference: none); 1: reflecting box after integration */
+    float box_lo[3];
+    float box_hi[3];
+    float restitution;             /* wall restitution (velocity scale on reflection) */
+    int32_t boundary_self_density; /* default 0: boundary-boundary predicted density stays zero, as the
+                                      reference never launches that kernel (Fluid.cpp:167-171); 1: computed */
+    int32_t loop_mode;             /* default 0: the corrective loop is decided on the device (CUDA graph with
+                                      a conditional while node); 1: host reads the decision each iteration,
+                                      like the reference (Fluid.cpp:300-306) */
+} pcisph_options;
+
+typedef struct pcisph_step_stats {
+    int32_t iterations;          /* corrective iterations of the last step */
+    float max_density_error;     /* max density variation / rest density, last iteration of the last step */
+    uint32_t status;             /* pcisph_step_status bits of the last step */
+    uint32_t status_all;         /* OR of the status bits of every step since the last reset */
+    uint64_t steps;              /* steps done by this context */
+    uint64_t total_iterations;   /* corrective iterations summed over those steps */
+} pcisph_step_stats;
+
+/* ----------------------------------------------------------- enums */
+enum pcisph_layout {
+    PCISPH_LAYOUT_PACKED3 = 0,  /* n x 3 floats (the reference's vload3/vstore3 layout) */
+    PCISPH_LAYOUT_FLOAT4 = 1,   /* n x 4 floats, w ignored on input, 0 on output */
+    PCISPH_LAYOUT_SCALAR = 2    /* n floats or n uint32 */
+};
+enum pcisph_memory { PCISPH_MEM_HOST = 0, PCISPH_MEM_DEVICE = 1 };
+
+enum pcisph_field {
+    PCISPH_FIELD_POSITION = 0,            /* particle state: after the last step, in its sorted order */
+    PCISPH_FIELD_VELOCITY = 1,
+    PCISPH_FIELD_NORMAL = 2,              /* Fluid.h:44 fluid_normals */
+    PCISPH_FIELD_PREDICTED_POSITION = 3,  /* fluid_predicted_positions */
+    PCISPH_FIELD_DENSITY = 4,             /* fluid_densities */
+    PCISPH_FIELD_OTHER_FORCE = 5,         /* fluid_other_forces */
+    PCISPH_FIELD_PRESSURE = 6,            /* fluid_pressures */
+    PCISPH_FIELD_PRESSURE_FORCE = 7,      /* fluid_pressure_forces */
+    PCISPH_FIELD_DENSITY_VARIATION = 8,   /* fluid_density_variations (internal, Fluid.h:99) */
+    PCISPH_FIELD_SORTED_POSITION = 9,     /* the step's positions after reorder */
+    PCISPH_FIELD_SORTED_VELOCITY = 10,
+    PCISPH_FIELD_KEYS = 11,               /* fluid_keys, sorted (uint32) */
+    PCISPH_FIELD_SRC = 12,                /* fluid_src_locations (uint32) */
+    PCISPH_FIELD_CELL_OFFSETS = 13,       /* fluid_cell_offsets, 2 x bucket_count uint32 */
+    PCISPH_FIELD_BOUNDARY_POSITION = 14,  /* boundary_positions, sorted once sorted */
+    PCISPH_FIELD_BOUNDARY_PRESSURE = 15,
+    PCISPH_FIELD_BOUNDARY_INIT_DENSITY = 16,
+    PCISPH_FIELD_BOUNDARY_KEYS = 17,
+    PCISPH_FIELD_BOUNDARY_SRC = 18,
+    PCISPH_FIELD_BOUNDARY_CELL_OFFSETS = 19,
+    PCISPH_FIELD_COUNT_ = 20
+};
+
+/* Single stages of the step, for parity testing of each kernel on given inputs. */
+enum pcisph_stage {
+    PCISPH_STAGE_SORT = 0,               /* boundary sort if pending, hash, radix sort, reorder + cell ranges */
+    PCISPH_STAGE_DENSITY = 1,            /* pcisph.cl:65-92 */
+    PCISPH_STAGE_NORMAL = 2,             /* pcisph.cl:94-112 */
+    PCISPH_STAGE_FORCE = 3,              /* pcisph.cl:121-173, then the first predict (pcisph.cl:175-193) */
+    PCISPH_STAGE_BOUNDARY_PRESSURE = 4,  /* pcisph.cl:212-263, boundary_update = 1 */
+    PCISPH_STAGE_PRESSURE = 5,           /* pcisph.cl:212-263, boundary_update = 0, + max reduction */
+    PCISPH_STAGE_PRESSURE_FORCE = 6,     /* pcisph.cl:265-300 then predict (arg 0) or integrate (arg 1) */
+    PCISPH_STAGE_PACK = 7,               /* rebuild packed operands from DENSITY, PRESSURE and
+                                            BOUNDARY_PRESSURE after set_field */
+    PCISPH_STAGE_BOUNDARY_PRESSURE_RESET = 8 /* pcisph.cl:114-119 */
+};
+
+typedef struct pcisph_ctx pcisph_ctx;
+
+/* ------------------------------------------------------------- general */
+PCISPH_API int pcisph_abi_version(void);
+PCISPH_API const char* pcisph_last_error(void);
+/* Setters + Fluid::update_deduced_attributes (Fluid.cpp:333-443) as a pure host function. */
+PCISPH_API int pcisph_derive_params(float particle_radius, float rest_density, uint32_t fluid_count, uint32_t boundary_count,
+                         float delta_t, float gravity, float viscosity, float surface_tension,
+                         pcisph_sim_params* out);
+/* Fluid.cpp:125-133 */
+PCISPH_API uint32_t pcisph_sort_bit_count(uint32_t elements);
+PCISPH_API int pcisph_default_options(pcisph_options* out);
+
+/* ------------------------------------------------------------ context */
+/* sim::Fluid::Fluid(ctx, device, queue) (Fluid.cpp:32-88). stream: cudaStream_t or NULL (legacy). */
+PCISPH_API int pcisph_create(int device, void* stream, pcisph_ctx** out);
+PCISPH_API void pcisph_destroy(pcisph_ctx* ctx);
+PCISPH_API int pcisph_set_stream(pcisph_ctx* ctx, void* stream);
+
+/* Setters, Fluid.h:21-29 (Fluid.cpp:333-375): each marks the parameters changed; the next update()
+ * re-derives them, reallocates and zeroes the velocities, like update_deduced_attributes. */
+PCISPH_API int pcisph_set_boundary_count(pcisph_ctx* ctx, uint32_t boundary_count);
+PCISPH_API int pcisph_set_fluid_count(pcisph_ctx* ctx, uint32_t fluid_count);
+PCISPH_API int pcisph_set_delta_t(pcisph_ctx* ctx, float delta_t);
+PCISPH_API int pcisph_set_rest_density(pcisph_ctx* ctx, float rest_density);
+PCISPH_API int pcisph_set_particle_radius(pcisph_ctx* ctx, float particle_radius);
+PCISPH_API int pcisph_set_gravity(pcisph_ctx* ctx, float gravity);
+PCISPH_API int pcisph_set_viscosity(pcisph_ctx* ctx, float viscosity);
+PCISPH_API int pcisph_set_surface_tension(pcisph_ctx* ctx, float surface_tension_coefficient);
+PCISPH_API int pcisph_set_density_variation_threshold(pcisph_ctx* ctx, float threshold);
+PCISPH_API int pcisph_set_options(pcisph_ctx* ctx, const pcisph_options* options);
+PCISPH_API int pcisph_get_options(const pcisph_ctx* ctx, pcisph_options* out);
+/* Fluid::get_params (Fluid.cpp:329-331): the current struct, derived fields as of the last derivation. */
+PCISPH_API int pcisph_get_params(const pcisph_ctx* ctx, pcisph_sim_params* out);
+/* Derive now if parameters changed (zeroing velocities), so that state set afterwards survives. */
+PCISPH_API int pcisph_prepare(pcisph_ctx* ctx);
+
+/* State import, replacing the caller-assigned cl::Buffers (scenes.cpp:191-208). count must equal the
+ * configured count (checked at update(), Fluid.cpp:90-106). vel may be NULL (zero). Stream-ordered. */
+PCISPH_API int pcisph_set_fluid_state(pcisph_ctx* ctx, const float* pos, const float* vel, uint32_t count, int layout,
+                           int memory);
+PCISPH_API int pcisph_set_boundary_state(pcisph_ctx* ctx, const float* pos, uint32_t count, int layout, int memory);
+/* Fluid::checkBuffersConsistent (Fluid.cpp:90-106) */
+PCISPH_API int pcisph_check_buffers_consistent(const pcisph_ctx* ctx);
+
+/* Fluid::update (Fluid.cpp:108-327): one time step, stream-ordered, no host synchronisation in
+ * loop_mode 0. */
+PCISPH_API int pcisph_update(pcisph_ctx* ctx);
+PCISPH_API int pcisph_step(pcisph_ctx* ctx, uint32_t steps);
+PCISPH_API int pcisph_sync(pcisph_ctx* ctx);
+/* Synchronises, then reports the last step. */
+PCISPH_API int pcisph_last_stats(pcisph_ctx* ctx, pcisph_step_stats* out);
+PCISPH_API int pcisph_reset_stats(pcisph_ctx* ctx);
+
+/* Export. dst_bytes must cover count x layout; HOST copies synchronise. */
+PCISPH_API int pcisph_get_field(pcisph_ctx* ctx, int field, void* dst, size_t dst_bytes, int layout, int memory);
+/* Overwrite one field (parity tests feed identical inputs to a stage). */
+PCISPH_API int pcisph_set_field(pcisph_ctx* ctx, int field, const void* src, size_t src_bytes, int layout, int memory);
+/* Zero-copy view (replaces the CL-GL shared buffers): device pointer, element count, native layout. */
+PCISPH_API int pcisph_field_device_ptr(pcisph_ctx* ctx, int field, void** ptr, size_t* count, int* layout);
+PCISPH_API int pcisph_run_stage(pcisph_ctx* ctx, int stage, int arg);
+
+/* Kernels launched by this context since creation (for launch accounting). */
+PCISPH_API uint64_t pcisph_kernel_launches(const pcisph_ctx* ctx);
+
+/* Per-kernel CUDA-event timing of the host-driven path (loop_mode 1 timing is used while enabled). */
+typedef struct pcisph_kernel_time {
+    char name[32];
+    uint64_t launches;
+    double total_ms;
+} pcisph_kernel_time;
+PCISPH_API int pcisph_profile_enable(pcisph_ctx* ctx, int enable);
+PCISPH_API int pcisph_profile_read(pcisph_ctx* ctx, pcisph_kernel_time* out, int max_entries, int* n_entries);
+
+/* --------------------------------------------------- standalone kernels */
+/* sort_utils.cl:12-23: key = hash(floor(pos / cell_size)) % bucket_count, id = index. Device pointers. */
+PCISPH_API int pcisph_hash_keys(const pcisph_sim_params* params, const float* pos, int layout, uint32_t count, uint32_t* keys,
+                     uint32_t* ids, void* stream);
+
+/* Replacement for clogs::Radixsort (radixsort.h:55-211): stable LSD radix sort of uint32 keys carrying
+ * uint32 values, on device pointers. max_bits 0 means 32; all keys must be < 2^max_bits. */
+typedef struct pcisph_radixsort pcisph_radixsort;
+PCISPH_API int pcisph_radixsort_create(int device, pcisph_radixsort** out);
+PCISPH_API void pcisph_radixsort_destroy(pcisph_radixsort* sorter);
+/* radixsort.h:186-191 */
+PCISPH_API int pcisph_radixsort_enqueue(pcisph_radixsort* sorter, uint32_t* keys, uint32_t* values, size_t elements,
+                             unsigned int max_bits, void* stream);
+/* Digit width in bits (4..11); 0 selects the tuned default. */
+PCISPH_API int pcisph_radixsort_set_digit_bits(pcisph_radixsort* sorter, int bits);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PCISPH_GPU_H */

@@ -1,0 +1,128 @@
+// common.cuh -- device-side vocabulary shared by the PCISPH kernels.
+//
+// Hashing is bit-exact with the reference (PCISPH/data/kernels/grid_utils.cl:9-19):
+//   cell = floor_sat(pos / cell_size)  (IEEE division, NaN -> 0, saturating)
+//   key  = ((((x*19349663) ^ (y*73856093) ^ (z*83492791)) << 6)
+//           + (x&63) + 4(y&63) + 16(z&63)) & 0x7FFFFFFF) % bucket_count
+// in wrapping 32-bit arithmetic. The modulo uses a precomputed multiplier
+// (Granlund & Montgomery, "Division by invariant integers using
+// multiplication", PLDI 1994, Thm 4.2): for n < 2^31 and l = ceil(log2 d),
+// m = ceil(2^(31+l) / d) < 2^32 gives floor(n/d) = umulhi(n, m) >> (l-1).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace pcisph {
+
+// Everything a step kernel needs, passed by value (lives in the constant bank).
+struct DevParams {
+    // reference fields (Simulation_Params)
+    float particle_mass, rest_density, h, h2, cell_size;
+    float poly6_norm, poly6_d1_norm, visc_d2_norm, spiky_d1_norm;
+    float st_coeff, st_term, st_norm, viscosity, gravity, dt, delta;
+    uint32_t fluid_count, boundary_count, bucket_count;
+    // modulo by bucket_count
+    uint32_t bk_magic, bk_shift;
+    // options
+    int min_iters, max_iters, walls;
+    float box_lo[3], box_hi[3], restitution, threshold;
+};
+
+struct Control {
+    unsigned int iter;           // iteration index within the current step
+    unsigned int max_err_bits;   // float bits of the running max density variation (>= 0)
+    unsigned int done;           // the loop stops after this iteration's pressure force
+    unsigned int blocks_done;    // last-block counter of the reduction
+    unsigned int status;         // pcisph_step_status bits of the current step
+    unsigned int status_all;
+    int iterations_last;
+    float max_err_last;          // max variation / rest density
+    unsigned long long steps;
+    unsigned long long total_iters;
+    unsigned int guard_iters;    // loop iterations counted by the pressure-force kernel (bounds the graph loop)
+};
+
+__host__ __device__ inline void magic_for(uint32_t d, uint32_t* magic, uint32_t* shift) {
+    uint32_t l = 0;
+    while (l < 32 && (1ull << l) < (unsigned long long)d) ++l;  // l = ceil(log2 d)
+    unsigned long long m = ((1ull << (31 + l)) + d - 1) / d;     // ceil(2^(31+l)/d), d >= 2
+    *magic = (uint32_t)m;
+    *shift = l - 1;
+}
+
+__device__ __forceinline__ uint32_t mod_bk(uint32_t v, const DevParams& P) {
+    uint32_t q = __umulhi(v, P.bk_magic) >> P.bk_shift;
+    return v - q * P.bucket_count;
+}
+
+// convert_int_sat_rtn
+__device__ __forceinline__ int floor_sat(float v) {
+    if (v != v) return 0;
+    float f = floorf(v);
+    if (f >= 2147483648.0f) return 0x7FFFFFFF;
+    if (f < -2147483648.0f) return (int)0x80000000;
+    return (int)f;
+}
+
+struct Cell {
+    uint32_t x, y, z;
+};
+
+__device__ __forceinline__ Cell cell_of(float px, float py, float pz, const DevParams& P) {
+    return Cell{(uint32_t)floor_sat(__fdiv_rn(px, P.cell_size)), (uint32_t)floor_sat(__fdiv_rn(py, P.cell_size)),
+                (uint32_t)floor_sat(__fdiv_rn(pz, P.cell_size))};
+}
+
+__device__ __forceinline__ uint32_t hash_key(uint32_t x, uint32_t y, uint32_t z, const DevParams& P) {
+    uint32_t h = (x * 19349663u) ^ (y * 73856093u) ^ (z * 83492791u);
+    uint32_t v = (h << 6) + (x & 63u) + 4u * (y & 63u) + 16u * (z & 63u);
+    return mod_bk(v & 0x7FFFFFFFu, P);
+}
+
+// The 27 neighbour buckets in the reference's walk order (grid_utils.cl:68-69: x fastest).
+// body(j) is called for every particle index j in every bucket; no bucket is skipped or merged.
+template <class Body>
+__device__ __forceinline__ void for_each_neighbour(const uint2* __restrict__ cells, const Cell& c,
+                                                   const DevParams& P, Body&& body) {
+#pragma unroll 1
+    for (int dz = -1; dz <= 1; ++dz) {
+        const uint32_t z = c.z + (uint32_t)dz;
+        const uint32_t hz = z * 83492791u, lz = 16u * (z & 63u);
+#pragma unroll 1
+        for (int dy = -1; dy <= 1; ++dy) {
+            const uint32_t y = c.y + (uint32_t)dy;
+            const uint32_t hyz = (y * 73856093u) ^ hz, lyz = 4u * (y & 63u) + lz;
+#pragma unroll
+            for (int dx = -1; dx <= 1; ++dx) {
+                const uint32_t x = c.x + (uint32_t)dx;
+                const uint32_t v = (((x * 19349663u) ^ hyz) << 6) + (x & 63u) + lyz;
+                const uint2 r = __ldg(&cells[mod_bk(v & 0x7FFFFFFFu, P)]);
+                for (uint32_t j = r.x; j < r.y; ++j) body(j);
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------- vectors
+__device__ __forceinline__ float3 f3(const float4& a) { return make_float3(a.x, a.y, a.z); }
+__device__ __forceinline__ float3 operator+(float3 a, float3 b) { return make_float3(a.x + b.x, a.y + b.y, a.z + b.z); }
+__device__ __forceinline__ float3 operator-(float3 a, float3 b) { return make_float3(a.x - b.x, a.y - b.y, a.z - b.z); }
+__device__ __forceinline__ float3 operator*(float3 a, float s) { return make_float3(a.x * s, a.y * s, a.z * s); }
+__device__ __forceinline__ float3 operator*(float s, float3 a) { return make_float3(s * a.x, s * a.y, s * a.z); }
+__device__ __forceinline__ float3 operator/(float3 a, float s) { return make_float3(a.x / s, a.y / s, a.z / s); }
+__device__ __forceinline__ float dot3(float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ float4 f4(float3 a, float w) { return make_float4(a.x, a.y, a.z, w); }
+
+// ------------------------------------------------------ smoothing kernels (pcisph.cl:8-61)
+__device__ __forceinline__ float poly6(float r2, float h2) {
+    const float dr = h2 - r2;
+    return r2 > h2 ? 0.f : dr * dr * dr;
+}
+__device__ __forceinline__ float surface_tension_kernel(float r, float h, float st_term) {
+    const float t1 = h - r;
+    const float t = (t1 * t1 * t1) * (r * r * r);
+    if (r <= 0.5f * h) return 2.f * t - st_term;
+    return r <= h ? t : 0.f;
+}
+
+}  // namespace pcisph

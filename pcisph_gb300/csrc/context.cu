@@ -1,0 +1,1055 @@
+// context.cu -- host driver of the PCISPH step and its C ABI (include/pcisph_gpu.h).
+//
+// pcisph_ctx plays the role of sim::Fluid (PCISPH/src/sim/Fluid.h:13-102):
+// parameter setters with lazy derivation (Fluid.cpp:333-443), a consistency
+// check (Fluid.cpp:90-106) and update() (Fluid.cpp:108-327). What differs is how
+// the step is scheduled on the GPU:
+//   - device memory lives in per-context arenas sized by the particle counts;
+//   - the fluid sort is the in-house radix sort (radix_sort.cu), keys bounded
+//     by bucket_count;
+//   - the corrective loop is decided on the device; by default the whole step is
+//     one CUDA graph whose loop is a conditional WHILE node, so a step costs one
+//     graph launch and no host synchronisation (loop_mode 0). loop_mode 1 reads
+//     the decision back every iteration, as the reference does (Fluid.cpp:300-306).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "../../include/pcisph_gpu.h"
+#include "common.cuh"
+#include "radix_sort.cuh"
+#include "step_kernels.cuh"
+
+using namespace pcisph;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string& msg) {
+    g_last_error = msg;
+    return code;
+}
+
+#define CUDA_TRY(call)                                                                                \
+    do {                                                                                              \
+        cudaError_t e_ = (call);                                                                      \
+        if (e_ != cudaSuccess) return fail(PCISPH_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
+
+const float kPi = 3.14159265358979323846f;  // utils/constants.h:4
+
+// Fluid.cpp:125-133
+uint32_t sort_bit_count_ref(uint32_t elements) {
+    uint32_t max_value = 0;
+    for (int i = 0; i < 32; i++) {
+        max_value = (max_value << 1) | 1u;
+        if (max_value >= elements - 1u) return (uint32_t)(i + 1);
+    }
+    return 32u;
+}
+
+// Bits needed for keys < bucket_count.
+int key_bits(uint32_t bucket_count) {
+    int b = 1;
+    while (b < 32 && (1ull << b) < (unsigned long long)bucket_count) ++b;
+    return b;
+}
+
+// update_deduced_attributes (Fluid.cpp:377-443): the same expressions, so the same floats.
+void derive(pcisph_sim_params* p) {
+    p->kernel_radius = 4.f * p->particle_radius;
+    p->kernel_radius2 = std::pow(p->kernel_radius, 2.f);
+    p->particle_mass = (float)((double)p->rest_density / std::pow((double)(1.f / (2.f * p->particle_radius)), 3.0));
+    p->bucket_count = p->fluid_count / 2;
+    p->bucket_count -= p->bucket_count % 64;
+    p->bucket_count = std::max(64u, p->bucket_count);
+    p->cell_size = p->kernel_radius;
+    p->poly6_normalization = 315.f / (64.f * kPi * std::pow(p->kernel_radius, 9.f));
+    p->poly6_d1_normalization = -945.f / (32.f * kPi * std::pow(p->kernel_radius, 9.f));
+    p->viscosity_d2_normalization = 45.f / (kPi * std::pow(p->kernel_radius, 6.0f));
+    p->spiky_d1_normalization = -45.f / (kPi * std::pow(p->kernel_radius, 6.0f));
+    p->surface_tension_normalization = 32.f / (kPi * std::pow(p->kernel_radius, 9.f));
+    p->surface_tension_term = std::pow(p->kernel_radius, 6.f) / 64.f;
+    const float particle_size = 2.f * p->particle_radius;
+    const float beta = p->delta_t * p->delta_t * p->particle_mass * p->particle_mass * 2.f /
+                       (p->rest_density * p->rest_density);
+    float sum[3] = {0.f, 0.f, 0.f}, sum_sq = 0.f;
+    const float lim = p->kernel_radius + particle_size;
+    for (float z = -p->kernel_radius - particle_size; z <= lim; z += 2.f * p->particle_radius)
+        for (float y = -p->kernel_radius - particle_size; y <= lim; y += 2.f * p->particle_radius)
+            for (float x = -p->kernel_radius - particle_size; x <= lim; x += 2.f * p->particle_radius) {
+                const float r = std::sqrt(x * x + y * y + z * z);
+                const float r2 = r * r;
+                if (r2 < p->kernel_radius2) {
+                    const float f = (float)((double)p->poly6_d1_normalization *
+                                            std::pow((double)(p->kernel_radius2 - r2), 2.0));
+                    const float v[3] = {-f * x, -f * y, -f * z};
+                    for (int i = 0; i < 3; i++) {
+                        sum[i] += v[i];
+                        sum_sq += v[i] * v[i];
+                    }
+                }
+            }
+    float sum_dot = 0.f;
+    for (int i = 0; i < 3; i++) sum_dot += sum[i] * sum[i];
+    p->density_variation_scaling_factor = -1.f / (beta * (-sum_dot - sum_sq));
+}
+
+struct DeviceGuard {
+    int prev = -1;
+    explicit DeviceGuard(int dev) {
+        cudaGetDevice(&prev);
+        if (prev != dev) cudaSetDevice(dev);
+    }
+    ~DeviceGuard() {
+        int cur = -1;
+        cudaGetDevice(&cur);
+        if (prev >= 0 && cur != prev) cudaSetDevice(prev);
+    }
+};
+
+struct DeviceBlock {
+    void* p = nullptr;
+    size_t cap = 0;
+    cudaError_t ensure(size_t bytes) {
+        if (bytes <= cap && p) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+        cudaError_t e = cudaMalloc(&p, std::max<size_t>(bytes, 256));
+        if (e == cudaSuccess) cap = std::max<size_t>(bytes, 256);
+        return e;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+    }
+};
+
+struct Carver {
+    unsigned char* base;
+    size_t off = 0;
+    template <class T>
+    T* take(size_t count) {
+        T* r = reinterpret_cast<T*>(base + off);
+        off += align256(count * sizeof(T));
+        return r;
+    }
+};
+
+size_t fluid_arena_bytes(uint32_t n, uint32_t bk) {
+    return 10 * align256((size_t)n * 16) + 3 * align256((size_t)n * 4) + 2 * align256((size_t)n * 4) +
+           align256((size_t)bk * 8);
+}
+size_t boundary_arena_bytes(uint32_t n, uint32_t bk) {
+    return 3 * align256((size_t)n * 16) + 4 * align256((size_t)n * 4) + align256((size_t)bk * 8);
+}
+
+struct KernelTiming {
+    uint64_t launches = 0;
+    double ms = 0.0;
+};
+
+}  // namespace
+
+struct pcisph_ctx {
+    int device = 0;
+    cudaStream_t user_stream = nullptr;  // launches go here (may be the legacy stream)
+    cudaStream_t capture_stream = nullptr;
+    pcisph_sim_params params{};
+    pcisph_options opts{};
+    float threshold = 0.01f;
+    bool params_changed = true;
+    bool boundary_updated = true;
+    uint32_t fluid_loaded = 0xFFFFFFFFu, boundary_loaded = 0xFFFFFFFFu;
+    uint32_t fluid_cap_n = 0, fluid_cap_bk = 0, boundary_cap_n = 0, boundary_cap_bk = 0;
+
+    DeviceBlock fluid_block, boundary_block, misc_block, sort_block, staging_block;
+    StepBuffers b{};
+    float4* b_pos_in = nullptr;
+    uint32_t *f_keys = nullptr, *f_ids = nullptr, *b_keys = nullptr, *b_ids = nullptr;
+    uint32_t *sorted_keys = nullptr, *sorted_ids = nullptr;
+    Control* ctl = nullptr;
+    Control* host_ctl = nullptr;  // pinned
+    RadixSorter sorter;
+    DevParams P{};
+
+    cudaGraphExec_t graph_exec = nullptr;
+    bool graph_valid = false;
+    uint64_t host_launches = 0;
+    uint64_t host_mode_iters = 0;  // corrective iterations run by the host-driven loop
+    cudaStream_t own_stream = nullptr;
+    uint64_t steps_launched = 0;
+    int prefix_launches = 0;
+    int iter_launches = 0;
+
+    bool profiling = false;
+    std::map<std::string, KernelTiming> timings;
+    struct Pending {
+        std::string name;
+        cudaEvent_t a, b;
+    };
+    std::vector<Pending> pending;
+    std::vector<cudaEvent_t> event_pool;
+
+    cudaStream_t stream() const { return user_stream; }
+
+    // ------------------------------------------------------------ memory
+    int ensure_fluid(uint32_t n, uint32_t bk) {
+        if (n == fluid_cap_n && bk == fluid_cap_bk && fluid_block.p) return PCISPH_OK;
+        CUDA_TRY(cudaStreamSynchronize(stream()));
+        if (fluid_block.ensure(fluid_arena_bytes(n, bk)) != cudaSuccess)
+            return fail(PCISPH_ERR_OOM, "device allocation of the fluid arena failed (" + std::to_string(n) +
+                                            " particles)");
+        Carver c{static_cast<unsigned char*>(fluid_block.p)};
+        b.state_pos = c.take<float4>(n);
+        b.state_vel = c.take<float4>(n);
+        b.pos = c.take<float4>(n);
+        b.vel = c.take<float4>(n);
+        b.pr4 = c.take<float4>(n);
+        b.normal = c.take<float4>(n);
+        b.f_other = c.take<float4>(n);
+        b.f_press = c.take<float4>(n);
+        b.pred = c.take<float4>(n);
+        b.pf4 = c.take<float4>(n);
+        b.rho = c.take<float>(n);
+        b.press = c.take<float>(n);
+        b.err = c.take<float>(n);
+        f_keys = c.take<uint32_t>(n);
+        f_ids = c.take<uint32_t>(n);
+        b.cells = c.take<uint2>(bk);
+        CUDA_TRY(cudaMemsetAsync(fluid_block.p, 0, fluid_arena_bytes(n, bk), stream()));
+        fluid_cap_n = n;
+        fluid_cap_bk = bk;
+        sorted_keys = f_keys;
+        sorted_ids = f_ids;
+        graph_valid = false;
+        return ensure_shared(std::max(n, boundary_cap_n));
+    }
+
+    int ensure_boundary(uint32_t n, uint32_t bk) {
+        if (n == boundary_cap_n && bk == boundary_cap_bk && boundary_block.p) return PCISPH_OK;
+        CUDA_TRY(cudaStreamSynchronize(stream()));
+        if (boundary_block.ensure(boundary_arena_bytes(n, bk)) != cudaSuccess)
+            return fail(PCISPH_ERR_OOM, "device allocation of the boundary arena failed");
+        Carver c{static_cast<unsigned char*>(boundary_block.p)};
+        b_pos_in = c.take<float4>(n);
+        b.b_pos = c.take<float4>(n);
+        b.bpf = c.take<float4>(n);
+        b.b_press = c.take<float>(n);
+        b.b_init = c.take<float>(n);
+        b_keys = c.take<uint32_t>(n);
+        b_ids = c.take<uint32_t>(n);
+        b.b_cells = c.take<uint2>(bk);
+        CUDA_TRY(cudaMemsetAsync(boundary_block.p, 0, boundary_arena_bytes(n, bk), stream()));
+        boundary_cap_n = n;
+        boundary_cap_bk = bk;
+        graph_valid = false;
+        return ensure_shared(std::max(n, fluid_cap_n));
+    }
+
+    int ensure_shared(uint32_t n) {
+        const size_t sort_bytes = RadixSorter::scratch_bytes(std::max<uint32_t>(n, 1), sorter.digit_bits());
+        if (sort_block.cap < sort_bytes) {
+            if (sort_block.ensure(sort_bytes) != cudaSuccess)
+                return fail(PCISPH_ERR_OOM, "device allocation of the sort scratch failed");
+            sorter.set_scratch(sort_block.p, sort_block.cap);
+            graph_valid = false;
+        }
+        if (staging_block.ensure((size_t)std::max<uint32_t>(n, 1) * 16) != cudaSuccess)
+            return fail(PCISPH_ERR_OOM, "device allocation of the staging buffer failed");
+        return PCISPH_OK;
+    }
+
+    // -------------------------------------------------------- parameters
+    void build_devparams() {
+        DevParams& d = P;
+        d.particle_mass = params.particle_mass;
+        d.rest_density = params.rest_density;
+        d.h = params.kernel_radius;
+        d.h2 = params.kernel_radius2;
+        d.cell_size = params.cell_size;
+        d.poly6_norm = params.poly6_normalization;
+        d.poly6_d1_norm = params.poly6_d1_normalization;
+        d.visc_d2_norm = params.viscosity_d2_normalization;
+        d.spiky_d1_norm = params.spiky_d1_normalization;
+        d.st_coeff = params.surface_tension_coefficient;
+        d.st_term = params.surface_tension_term;
+        d.st_norm = params.surface_tension_normalization;
+        d.viscosity = params.viscosity_constant;
+        d.gravity = params.gravity;
+        d.dt = params.delta_t;
+        d.delta = params.density_variation_scaling_factor;
+        d.fluid_count = params.fluid_count;
+        d.boundary_count = params.boundary_count;
+        d.bucket_count = params.bucket_count;
+        magic_for(params.bucket_count, &d.bk_magic, &d.bk_shift);
+        d.min_iters = opts.min_iterations;
+        d.max_iters = opts.max_iterations;
+        d.walls = opts.walls;
+        for (int a = 0; a < 3; a++) {
+            d.box_lo[a] = opts.box_lo[a];
+            d.box_hi[a] = opts.box_hi[a];
+        }
+        d.restitution = opts.restitution;
+        d.threshold = threshold;
+        graph_valid = false;
+    }
+
+    // update_deduced_attributes: derive, (re)allocate, zero velocities, mark the boundary for sorting.
+    int derive_now() {
+        derive(&params);
+        int rc = ensure_fluid(params.fluid_count, params.bucket_count);
+        if (rc) return rc;
+        rc = ensure_boundary(params.boundary_count, params.bucket_count);
+        if (rc) return rc;
+        if (params.fluid_count) CUDA_TRY(cudaMemsetAsync(b.state_vel, 0, (size_t)params.fluid_count * 16, stream()));
+        build_devparams();
+        boundary_updated = true;
+        params_changed = false;
+        return PCISPH_OK;
+    }
+
+    // -------------------------------------------------------------- timing
+    cudaEvent_t take_event() {
+        if (!event_pool.empty()) {
+            cudaEvent_t e = event_pool.back();
+            event_pool.pop_back();
+            return e;
+        }
+        cudaEvent_t e;
+        cudaEventCreate(&e);
+        return e;
+    }
+    template <class F>
+    void timed(const char* name, cudaStream_t s, F&& f) {
+        if (!profiling) {
+            f();
+            return;
+        }
+        Pending p{name, take_event(), take_event()};
+        cudaEventRecord(p.a, s);
+        f();
+        cudaEventRecord(p.b, s);
+        pending.push_back(p);
+    }
+    void collect_timings() {
+        if (pending.empty()) return;
+        cudaStreamSynchronize(stream());
+        for (auto& p : pending) {
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, p.a, p.b);
+            auto& t = timings[p.name];
+            t.launches += 1;
+            t.ms += ms;
+            event_pool.push_back(p.a);
+            event_pool.push_back(p.b);
+        }
+        pending.clear();
+    }
+
+    // ---------------------------------------------------------------- sort
+    int sort_set(const float4* pos_in, uint32_t n, uint32_t* keys, uint32_t* ids, uint32_t** sk, uint32_t** sv,
+                 cudaStream_t s) {
+        timed("hash", s, [&] { launch_hash(reinterpret_cast<const float*>(pos_in), false, n, P, keys, nullptr, s); });
+        int nl = 0;
+        cudaError_t e = cudaSuccess;
+        timed("radix_sort", s, [&] {
+            e = sorter.sort(keys, ids, n, key_bits(params.bucket_count), true, s, sk, sv);
+            nl = sorter.last_launches();
+        });
+        if (e != cudaSuccess) {
+            fail(PCISPH_ERR_CUDA, std::string("radix sort: ") + cudaGetErrorString(e));
+            return -1;
+        }
+        return 1 + nl;
+    }
+
+    int boundary_sort(cudaStream_t s) {
+        const uint32_t B = params.boundary_count;
+        CUDA_TRY(cudaMemsetAsync(b.b_cells, 0, (size_t)params.bucket_count * 8, s));
+        uint32_t *sk = nullptr, *sv = nullptr;
+        int nl = sort_set(b_pos_in, B, b_keys, b_ids, &sk, &sv, s);
+        if (nl < 0) return PCISPH_ERR_CUDA;
+        if (sk != b_keys) {
+            CUDA_TRY(cudaMemcpyAsync(b_keys, sk, (size_t)B * 4, cudaMemcpyDeviceToDevice, s));
+            CUDA_TRY(cudaMemcpyAsync(b_ids, sv, (size_t)B * 4, cudaMemcpyDeviceToDevice, s));
+        }
+        timed("reorder_boundary", s,
+              [&] { launch_reorder(b_keys, b_ids, b_pos_in, nullptr, B, b.b_pos, nullptr, b.b_cells, params.bucket_count, b.ctl, s); });
+        if (opts.boundary_self_density) timed("boundary_self_density", s, [&] { launch_boundary_self_density(P, b, s); });
+        else CUDA_TRY(cudaMemsetAsync(b.b_init, 0, (size_t)B * 4, s));
+        host_launches += nl + 1 + (opts.boundary_self_density ? 1 : 0);
+        CUDA_TRY(cudaGetLastError());
+        boundary_updated = false;
+        return PCISPH_OK;
+    }
+
+    // ---------------------------------------------------------------- step
+    // Everything before the corrective loop. Returns the number of kernels, or -1 on error.
+    int record_prefix(cudaStream_t s) {
+        const uint32_t N = params.fluid_count, B = params.boundary_count;
+        int nl = 0;
+        launch_begin(b.ctl, s);
+        ++nl;
+        if (cudaMemsetAsync(b.cells, 0, (size_t)params.bucket_count * 8, s) != cudaSuccess) return -1;
+        uint32_t *sk = nullptr, *sv = nullptr;
+        int r = sort_set(b.state_pos, N, f_keys, f_ids, &sk, &sv, s);
+        if (r < 0) return -1;
+        nl += r;
+        sorted_keys = sk;
+        sorted_ids = sv;
+        timed("reorder", s, [&] { launch_reorder(sk, sv, b.state_pos, b.state_vel, N, b.pos, b.vel, b.cells, params.bucket_count, b.ctl, s); });
+        timed("density", s, [&] { launch_density(P, b, s); });
+        timed("normal", s, [&] { launch_normal(P, b, s); });
+        if (B && cudaMemsetAsync(b.b_press, 0, (size_t)B * 4, s) != cudaSuccess) return -1;
+        timed("force", s, [&] { launch_force(P, b, s); });
+        nl += 4;
+        if (cudaGetLastError() != cudaSuccess) return -1;
+        return nl;
+    }
+
+    int record_iteration(cudaStream_t s, cudaGraphConditionalHandle cond, bool use_cond) {
+        int nl = 0;
+        if (params.boundary_count) {
+            timed("boundary_pressure", s, [&] { launch_boundary_pressure(P, b, s); });
+            ++nl;
+        }
+        timed("pressure", s, [&] { launch_pressure(P, b, s); });
+        timed("pressure_force", s, [&] { launch_pressure_force(P, b, 0, cond, use_cond, s); });
+        nl += 2;
+        return nl;
+    }
+
+    int build_graph() {
+        if (graph_exec) {
+            cudaGraphExecDestroy(graph_exec);
+            graph_exec = nullptr;
+        }
+        const bool prof = profiling;
+        profiling = false;
+        cudaStream_t s = capture_stream;
+        cudaGraph_t graph = nullptr;
+        CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        int nl = record_prefix(s);
+        cudaStreamCaptureStatus st;
+        const cudaGraphNode_t* deps = nullptr;
+        size_t ndeps = 0;
+        cudaError_t e = cudaStreamGetCaptureInfo(s, &st, nullptr, nullptr, &deps, nullptr, &ndeps);
+        std::vector<cudaGraphNode_t> leaves(deps, deps + (e == cudaSuccess ? ndeps : 0));
+        cudaError_t e2 = cudaStreamEndCapture(s, &graph);
+        profiling = prof;
+        if (nl < 0 || e != cudaSuccess || e2 != cudaSuccess) {
+            if (graph) cudaGraphDestroy(graph);
+            return fail(PCISPH_ERR_CUDA, std::string("graph capture of the step failed: ") +
+                                             cudaGetErrorString(e != cudaSuccess ? e : e2));
+        }
+        prefix_launches = nl;
+        cudaGraphConditionalHandle handle;
+        CUDA_TRY(cudaGraphConditionalHandleCreate(&handle, graph, 1, cudaGraphCondAssignDefault));
+        cudaGraphNodeParams cp{};
+        cp.type = cudaGraphNodeTypeConditional;
+        cp.conditional.handle = handle;
+        cp.conditional.type = cudaGraphCondTypeWhile;
+        cp.conditional.size = 1;
+        cudaGraphNode_t loop_node;
+        CUDA_TRY(cudaGraphAddNode(&loop_node, graph, leaves.data(), nullptr, leaves.size(), &cp));
+        cudaGraph_t body = cp.conditional.phGraph_out[0];
+        CUDA_TRY(cudaStreamBeginCaptureToGraph(s, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+        profiling = false;
+        iter_launches = record_iteration(s, handle, true);
+        profiling = prof;
+        cudaGraph_t body_out = nullptr;
+        CUDA_TRY(cudaStreamEndCapture(s, &body_out));
+        e = cudaGraphInstantiate(&graph_exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) return fail(PCISPH_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+        graph_valid = true;
+        return PCISPH_OK;
+    }
+
+    int check_consistent() const {
+        if (params.fluid_count == 0) return PCISPH_OK;
+        auto msg = [&](const char* name, uint32_t got) {
+            return std::string("Inconsistent ") + name + " (" + std::to_string(got) + ") for " +
+                   std::to_string(params.fluid_count) + " particles";
+        };
+        if (fluid_loaded != params.fluid_count)
+            return fail(PCISPH_ERR_INCONSISTENT, msg("positions_size", fluid_loaded == 0xFFFFFFFFu ? 0 : fluid_loaded));
+        if (params.boundary_count && boundary_loaded != params.boundary_count)
+            return fail(PCISPH_ERR_INCONSISTENT, "Inconsistent boundary_positions (" +
+                                                     std::to_string(boundary_loaded == 0xFFFFFFFFu ? 0 : boundary_loaded) +
+                                                     ") for " + std::to_string(params.boundary_count) + " particles");
+        return PCISPH_OK;
+    }
+
+    int update() {
+        if (params_changed) {
+            int rc = derive_now();
+            if (rc) return rc;
+        }
+        int rc = check_consistent();
+        if (rc) return rc;
+        if (params.fluid_count == 0) return PCISPH_OK;  // Fluid.cpp:117-118
+        cudaStream_t s = stream();
+        if (boundary_updated && params.boundary_count > 0) {
+            rc = boundary_sort(s);
+            if (rc) return rc;
+        }
+        if (opts.loop_mode == 0 && !profiling) {
+            if (!graph_valid) {
+                rc = build_graph();
+                if (rc) return rc;
+            }
+            CUDA_TRY(cudaGraphLaunch(graph_exec, s));
+            host_launches += prefix_launches;
+            ++steps_launched;
+            return PCISPH_OK;
+        }
+        // host-driven loop (Fluid.cpp:250-307)
+        int nl = record_prefix(s);
+        if (nl < 0) return fail(PCISPH_ERR_CUDA, std::string("step launch failed: ") + cudaGetErrorString(cudaGetLastError()));
+        host_launches += nl;
+        ++steps_launched;
+        const int lim = std::max(1, opts.max_iterations);
+        for (int i = 0; i < lim; ++i) {
+            host_launches += record_iteration(s, 0, false);
+            ++host_mode_iters;
+            CUDA_TRY(cudaGetLastError());
+            if (i + 1 >= std::min(opts.min_iterations, lim)) {
+                CUDA_TRY(cudaMemcpyAsync(&host_ctl->done, &b.ctl->done, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+                CUDA_TRY(cudaStreamSynchronize(s));
+                if (host_ctl->done) break;
+            }
+        }
+        collect_timings();
+        return PCISPH_OK;
+    }
+
+    int run_stage(int stage, int arg) {
+        if (params_changed) {
+            int rc = derive_now();
+            if (rc) return rc;
+        }
+        int rc = check_consistent();
+        if (rc) return rc;
+        cudaStream_t s = stream();
+        const uint32_t N = params.fluid_count;
+        switch (stage) {
+            case PCISPH_STAGE_SORT: {
+                if (boundary_updated && params.boundary_count > 0) {
+                    rc = boundary_sort(s);
+                    if (rc) return rc;
+                }
+                launch_begin(b.ctl, s);
+                CUDA_TRY(cudaMemsetAsync(b.cells, 0, (size_t)params.bucket_count * 8, s));
+                uint32_t *sk = nullptr, *sv = nullptr;
+                int nl = sort_set(b.state_pos, N, f_keys, f_ids, &sk, &sv, s);
+                if (nl < 0) return PCISPH_ERR_CUDA;
+                sorted_keys = sk;
+                sorted_ids = sv;
+                launch_reorder(sk, sv, b.state_pos, b.state_vel, N, b.pos, b.vel, b.cells, params.bucket_count, b.ctl, s);
+                host_launches += nl + 2;
+                break;
+            }
+            case PCISPH_STAGE_DENSITY: launch_density(P, b, s); ++host_launches; break;
+            case PCISPH_STAGE_NORMAL: launch_normal(P, b, s); ++host_launches; break;
+            case PCISPH_STAGE_FORCE: launch_force(P, b, s); ++host_launches; break;
+            case PCISPH_STAGE_BOUNDARY_PRESSURE: launch_boundary_pressure(P, b, s); ++host_launches; break;
+            case PCISPH_STAGE_PRESSURE: launch_pressure(P, b, s); ++host_launches; break;
+            case PCISPH_STAGE_PRESSURE_FORCE: launch_pressure_force(P, b, arg ? 2 : 1, 0, false, s); ++host_launches; break;
+            case PCISPH_STAGE_PACK: launch_pack(P, b, s); ++host_launches; break;
+            case PCISPH_STAGE_BOUNDARY_PRESSURE_RESET:
+                if (params.boundary_count) CUDA_TRY(cudaMemsetAsync(b.b_press, 0, (size_t)params.boundary_count * 4, s));
+                break;
+            default: return fail(PCISPH_ERR_INVALID_ARG, "unknown stage " + std::to_string(stage));
+        }
+        CUDA_TRY(cudaGetLastError());
+        return PCISPH_OK;
+    }
+
+    // ---------------------------------------------------------------- fields
+    struct FieldView {
+        void* ptr;
+        size_t count;      // elements (particles, or uint32 entries for tables)
+        int layout;        // native: FLOAT4 or SCALAR
+    };
+    bool field_view(int field, FieldView* v) {
+        const size_t N = params.fluid_count, B = params.boundary_count, BK = params.bucket_count;
+        switch (field) {
+            case PCISPH_FIELD_POSITION: *v = {b.state_pos, N, PCISPH_LAYOUT_FLOAT4}; return true;
+            case PCISPH_FIELD_VELOCITY: *v = {b.state_vel, N, PCISPH_LAYOUT_FLOAT4}; return true;
+            case PCISPH_FIELD_NORMAL: *v = {b.normal, N, PCISPH_LAYOUT_FLOAT4}; return true;
+            case PCISPH_FIELD_PREDICTED_POSITION: *v = {b.pred, N, PCISPH_LAYOUT_FLOAT4}; return true;
+            case PCISPH_FIELD_DENSITY: *v = {b.rho, N, PCISPH_LAYOUT_SCALAR}; return true;
+            case PCISPH_FIELD_OTHER_FORCE: *v = {b.f_other, N, PCISPH_LAYOUT_FLOAT4}; return true;
+            case PCISPH_FIELD_PRESSURE: *v = {b.press, N, PCISPH_LAYOUT_SCALAR}; return true;
+            case PCISPH_FIELD_PRESSURE_FORCE: *v = {b.f_press, N, PCISPH_LAYOUT_FLOAT4}; return true;
+            case PCISPH_FIELD_DENSITY_VARIATION: *v = {b.err, N, PCISPH_LAYOUT_SCALAR}; return true;
+            case PCISPH_FIELD_SORTED_POSITION: *v = {b.pos, N, PCISPH_LAYOUT_FLOAT4}; return true;
+            case PCISPH_FIELD_SORTED_VELOCITY: *v = {b.vel, N, PCISPH_LAYOUT_FLOAT4}; return true;
+            case PCISPH_FIELD_KEYS: *v = {sorted_keys, N, PCISPH_LAYOUT_SCALAR}; return true;
+            case PCISPH_FIELD_SRC: *v = {sorted_ids, N, PCISPH_LAYOUT_SCALAR}; return true;
+            case PCISPH_FIELD_CELL_OFFSETS: *v = {b.cells, 2 * BK, PCISPH_LAYOUT_SCALAR}; return true;
+            case PCISPH_FIELD_BOUNDARY_POSITION: *v = {b.b_pos, B, PCISPH_LAYOUT_FLOAT4}; return true;
+            case PCISPH_FIELD_BOUNDARY_PRESSURE: *v = {b.b_press, B, PCISPH_LAYOUT_SCALAR}; return true;
+            case PCISPH_FIELD_BOUNDARY_INIT_DENSITY: *v = {b.b_init, B, PCISPH_LAYOUT_SCALAR}; return true;
+            case PCISPH_FIELD_BOUNDARY_KEYS: *v = {b_keys, B, PCISPH_LAYOUT_SCALAR}; return true;
+            case PCISPH_FIELD_BOUNDARY_SRC: *v = {b_ids, B, PCISPH_LAYOUT_SCALAR}; return true;
+            case PCISPH_FIELD_BOUNDARY_CELL_OFFSETS: *v = {b.b_cells, 2 * BK, PCISPH_LAYOUT_SCALAR}; return true;
+            default: return false;
+        }
+    }
+
+    static size_t layout_bytes(size_t count, int layout) {
+        return count * (layout == PCISPH_LAYOUT_PACKED3 ? 12 : layout == PCISPH_LAYOUT_FLOAT4 ? 16 : 4);
+    }
+
+    int copy_vectors_in(float4* dst, const float* src, size_t n, int layout, int memory) {
+        cudaStream_t s = stream();
+        if (n == 0) return PCISPH_OK;
+        if (layout == PCISPH_LAYOUT_FLOAT4) {
+            CUDA_TRY(cudaMemcpyAsync(dst, src, n * 16,
+                                     memory == PCISPH_MEM_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice, s));
+        } else if (layout == PCISPH_LAYOUT_PACKED3) {
+            const float* dsrc = src;
+            if (memory == PCISPH_MEM_HOST) {
+                CUDA_TRY(cudaMemcpyAsync(staging_block.p, src, n * 12, cudaMemcpyHostToDevice, s));
+                dsrc = static_cast<const float*>(staging_block.p);
+            }
+            launch_pack3_to4(dsrc, dst, (uint32_t)n, s);
+            ++host_launches;
+            CUDA_TRY(cudaGetLastError());
+        } else {
+            return fail(PCISPH_ERR_INVALID_ARG, "vector fields take PACKED3 or FLOAT4");
+        }
+        return PCISPH_OK;
+    }
+
+    int get_field(int field, void* dst, size_t dst_bytes, int layout, int memory) {
+        FieldView v;
+        if (!field_view(field, &v)) return fail(PCISPH_ERR_INVALID_ARG, "unknown field " + std::to_string(field));
+        if (!v.ptr) return fail(PCISPH_ERR_NOT_READY, "field not allocated yet (set the state or call update first)");
+        if (v.layout == PCISPH_LAYOUT_SCALAR && layout != PCISPH_LAYOUT_SCALAR)
+            return fail(PCISPH_ERR_INVALID_ARG, "scalar field: use PCISPH_LAYOUT_SCALAR");
+        if (v.layout == PCISPH_LAYOUT_FLOAT4 && layout == PCISPH_LAYOUT_SCALAR)
+            return fail(PCISPH_ERR_INVALID_ARG, "vector field: use PACKED3 or FLOAT4");
+        const size_t need = layout_bytes(v.count, layout);
+        if (dst_bytes < need || (!dst && need))
+            return fail(PCISPH_ERR_INVALID_ARG, "destination too small: need " + std::to_string(need) + " bytes");
+        if (need == 0) return PCISPH_OK;
+        cudaStream_t s = stream();
+        const cudaMemcpyKind kind = memory == PCISPH_MEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+        if (layout == PCISPH_LAYOUT_PACKED3) {
+            float* out = memory == PCISPH_MEM_HOST ? static_cast<float*>(staging_block.p) : static_cast<float*>(dst);
+            launch_unpack4_to3(static_cast<const float4*>(v.ptr), out, (uint32_t)v.count, s);
+            ++host_launches;
+            CUDA_TRY(cudaGetLastError());
+            if (memory == PCISPH_MEM_HOST) CUDA_TRY(cudaMemcpyAsync(dst, out, need, kind, s));
+        } else {
+            CUDA_TRY(cudaMemcpyAsync(dst, v.ptr, need, kind, s));
+        }
+        if (memory == PCISPH_MEM_HOST) CUDA_TRY(cudaStreamSynchronize(s));
+        return PCISPH_OK;
+    }
+
+    int set_field(int field, const void* src, size_t src_bytes, int layout, int memory) {
+        FieldView v;
+        if (!field_view(field, &v)) return fail(PCISPH_ERR_INVALID_ARG, "unknown field " + std::to_string(field));
+        if (!v.ptr) return fail(PCISPH_ERR_NOT_READY, "field not allocated yet");
+        const size_t need = layout_bytes(v.count, layout);
+        if (src_bytes < need || (!src && need)) return fail(PCISPH_ERR_INVALID_ARG, "source too small");
+        if (v.layout == PCISPH_LAYOUT_FLOAT4)
+            return copy_vectors_in(static_cast<float4*>(v.ptr), static_cast<const float*>(src), v.count, layout, memory);
+        if (layout != PCISPH_LAYOUT_SCALAR) return fail(PCISPH_ERR_INVALID_ARG, "scalar field: use PCISPH_LAYOUT_SCALAR");
+        CUDA_TRY(cudaMemcpyAsync(v.ptr, src, need,
+                                 memory == PCISPH_MEM_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice,
+                                 stream()));
+        if (memory == PCISPH_MEM_HOST) CUDA_TRY(cudaStreamSynchronize(stream()));
+        return PCISPH_OK;
+    }
+
+    int stats(pcisph_step_stats* out) {
+        CUDA_TRY(cudaStreamSynchronize(stream()));
+        CUDA_TRY(cudaMemcpy(host_ctl, b.ctl, sizeof(Control), cudaMemcpyDeviceToHost));
+        out->iterations = host_ctl->iterations_last;
+        out->max_density_error = host_ctl->max_err_last;
+        out->status = host_ctl->status;
+        out->status_all = host_ctl->status_all;
+        out->steps = host_ctl->steps;
+        out->total_iterations = host_ctl->total_iters;
+        return PCISPH_OK;
+    }
+
+    ~pcisph_ctx() {
+        DeviceGuard g(device);
+        if (user_stream) cudaStreamSynchronize(user_stream);
+        if (graph_exec) cudaGraphExecDestroy(graph_exec);
+        for (auto& p : pending) {
+            cudaEventDestroy(p.a);
+            cudaEventDestroy(p.b);
+        }
+        for (auto e : event_pool) cudaEventDestroy(e);
+        fluid_block.release();
+        boundary_block.release();
+        misc_block.release();
+        sort_block.release();
+        staging_block.release();
+        if (host_ctl) cudaFreeHost(host_ctl);
+        if (capture_stream) cudaStreamDestroy(capture_stream);
+        if (own_stream) cudaStreamDestroy(own_stream);
+    }
+};
+
+// ====================================================================== C ABI
+extern "C" {
+
+int pcisph_abi_version(void) { return PCISPH_ABI_VERSION; }
+
+const char* pcisph_last_error(void) { return g_last_error.c_str(); }
+
+uint32_t pcisph_sort_bit_count(uint32_t elements) { return sort_bit_count_ref(elements); }
+
+int pcisph_derive_params(float particle_radius, float rest_density, uint32_t fluid_count, uint32_t boundary_count,
+                         float delta_t, float gravity, float viscosity, float surface_tension,
+                         pcisph_sim_params* out) {
+    if (!out) return fail(PCISPH_ERR_INVALID_ARG, "out is NULL");
+    std::memset(out, 0, sizeof(*out));
+    out->particle_radius = particle_radius;
+    out->rest_density = rest_density;
+    out->fluid_count = fluid_count;
+    out->boundary_count = boundary_count;
+    out->delta_t = delta_t;
+    out->gravity = gravity;
+    out->viscosity_constant = viscosity;
+    out->surface_tension_coefficient = surface_tension;
+    derive(out);
+    return PCISPH_OK;
+}
+
+int pcisph_default_options(pcisph_options* o) {
+    if (!o) return fail(PCISPH_ERR_INVALID_ARG, "out is NULL");
+    std::memset(o, 0, sizeof(*o));
+    o->min_iterations = 3;
+    o->max_iterations = 7;
+    o->walls = 0;
+    o->restitution = 0.5f;
+    o->boundary_self_density = 0;
+    o->loop_mode = 0;
+    return PCISPH_OK;
+}
+
+int pcisph_create(int device, void* stream, pcisph_ctx** out) {
+    if (!out) return fail(PCISPH_ERR_INVALID_ARG, "out is NULL");
+    *out = nullptr;
+    int ndev = 0;
+    CUDA_TRY(cudaGetDeviceCount(&ndev));
+    if (device < 0 || device >= ndev) return fail(PCISPH_ERR_INVALID_ARG, "no CUDA device " + std::to_string(device));
+    DeviceGuard g(device);
+    CUDA_TRY(cudaFree(nullptr));  // create the primary context
+    CUDA_TRY(radix_configure_kernels());
+    pcisph_ctx* c = new pcisph_ctx();
+    c->device = device;
+    pcisph_default_options(&c->opts);
+    c->params.rest_density = 1000.f;
+    cudaError_t e = cudaStreamCreateWithFlags(&c->capture_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMallocHost(&c->host_ctl, sizeof(Control));
+    if (e == cudaSuccess) e = c->misc_block.ensure(sizeof(Control));
+    if (e == cudaSuccess) e = cudaMemset(c->misc_block.p, 0, sizeof(Control));
+    if (e != cudaSuccess) {
+        delete c;
+        return fail(PCISPH_ERR_CUDA, std::string("context setup: ") + cudaGetErrorString(e));
+    }
+    c->user_stream = stream ? static_cast<cudaStream_t>(stream) : c->own_stream;
+    c->b.ctl = c->ctl = static_cast<Control*>(c->misc_block.p);
+    std::memset(c->host_ctl, 0, sizeof(Control));
+    *out = c;
+    return PCISPH_OK;
+}
+
+void pcisph_destroy(pcisph_ctx* ctx) { delete ctx; }
+
+int pcisph_set_stream(pcisph_ctx* ctx, void* stream) {
+    if (!ctx) return fail(PCISPH_ERR_INVALID_ARG, "ctx is NULL");
+    DeviceGuard g(ctx->device);
+    cudaStreamSynchronize(ctx->user_stream);
+    ctx->user_stream = stream ? static_cast<cudaStream_t>(stream) : ctx->own_stream;
+    return PCISPH_OK;
+}
+
+#define CTX_SETTER(name, field, type)                                   \
+    int name(pcisph_ctx* ctx, type v) {                                 \
+        if (!ctx) return fail(PCISPH_ERR_INVALID_ARG, "ctx is NULL");   \
+        ctx->params.field = v;                                          \
+        ctx->params_changed = true;                                     \
+        return PCISPH_OK;                                               \
+    }
+CTX_SETTER(pcisph_set_boundary_count, boundary_count, uint32_t)
+CTX_SETTER(pcisph_set_fluid_count, fluid_count, uint32_t)
+CTX_SETTER(pcisph_set_delta_t, delta_t, float)
+CTX_SETTER(pcisph_set_rest_density, rest_density, float)
+CTX_SETTER(pcisph_set_particle_radius, particle_radius, float)
+CTX_SETTER(pcisph_set_gravity, gravity, float)
+CTX_SETTER(pcisph_set_viscosity, viscosity_constant, float)
+CTX_SETTER(pcisph_set_surface_tension, surface_tension_coefficient, float)
+
+int pcisph_set_density_variation_threshold(pcisph_ctx* ctx, float t) {  // Fluid.cpp:373-375: no re-derivation
+    if (!ctx) return fail(PCISPH_ERR_INVALID_ARG, "ctx is NULL");
+    ctx->threshold = t;
+    ctx->P.threshold = t;
+    ctx->graph_valid = false;
+    return PCISPH_OK;
+}
+
+int pcisph_set_options(pcisph_ctx* ctx, const pcisph_options* o) {
+    if (!ctx || !o) return fail(PCISPH_ERR_INVALID_ARG, "NULL argument");
+    if (o->max_iterations < 1 || o->min_iterations < 1 || o->max_iterations > 10000)
+        return fail(PCISPH_ERR_INVALID_ARG, "iteration limits must be in 1..10000");
+    if (o->loop_mode != 0 && o->loop_mode != 1) return fail(PCISPH_ERR_INVALID_ARG, "loop_mode must be 0 or 1");
+    const bool bsd_changed = o->boundary_self_density != ctx->opts.boundary_self_density;
+    ctx->opts = *o;
+    if (bsd_changed) ctx->boundary_updated = true;
+    if (!ctx->params_changed) ctx->build_devparams();
+    return PCISPH_OK;
+}
+
+int pcisph_get_options(const pcisph_ctx* ctx, pcisph_options* out) {
+    if (!ctx || !out) return fail(PCISPH_ERR_INVALID_ARG, "NULL argument");
+    *out = ctx->opts;
+    return PCISPH_OK;
+}
+
+int pcisph_get_params(const pcisph_ctx* ctx, pcisph_sim_params* out) {
+    if (!ctx || !out) return fail(PCISPH_ERR_INVALID_ARG, "NULL argument");
+    *out = ctx->params;
+    return PCISPH_OK;
+}
+
+int pcisph_prepare(pcisph_ctx* ctx) {
+    if (!ctx) return fail(PCISPH_ERR_INVALID_ARG, "ctx is NULL");
+    DeviceGuard g(ctx->device);
+    return ctx->params_changed ? ctx->derive_now() : PCISPH_OK;
+}
+
+int pcisph_set_fluid_state(pcisph_ctx* ctx, const float* pos, const float* vel, uint32_t count, int layout,
+                           int memory) {
+    if (!ctx) return fail(PCISPH_ERR_INVALID_ARG, "ctx is NULL");
+    if (count && !pos) return fail(PCISPH_ERR_INVALID_ARG, "pos is NULL");
+    if (layout != PCISPH_LAYOUT_PACKED3 && layout != PCISPH_LAYOUT_FLOAT4)
+        return fail(PCISPH_ERR_INVALID_ARG, "positions take PACKED3 or FLOAT4");
+    if (memory != PCISPH_MEM_HOST && memory != PCISPH_MEM_DEVICE) return fail(PCISPH_ERR_INVALID_ARG, "bad memory kind");
+    if (count != ctx->params.fluid_count)
+        return fail(PCISPH_ERR_INCONSISTENT, "Inconsistent positions_size (" + std::to_string(count) + ") for " +
+                                                 std::to_string(ctx->params.fluid_count) + " particles");
+    DeviceGuard g(ctx->device);
+    uint32_t bk = ctx->params.fluid_count / 2;
+    bk -= bk % 64;
+    bk = std::max(64u, bk);
+    int rc = ctx->ensure_fluid(count, bk);
+    if (rc) return rc;
+    rc = ctx->copy_vectors_in(ctx->b.state_pos, pos, count, layout, memory);
+    if (rc) return rc;
+    if (vel) rc = ctx->copy_vectors_in(ctx->b.state_vel, vel, count, layout, memory);
+    else if (count) CUDA_TRY(cudaMemsetAsync(ctx->b.state_vel, 0, (size_t)count * 16, ctx->stream()));
+    if (rc) return rc;
+    if (memory == PCISPH_MEM_HOST) CUDA_TRY(cudaStreamSynchronize(ctx->stream()));
+    ctx->fluid_loaded = count;
+    return PCISPH_OK;
+}
+
+int pcisph_set_boundary_state(pcisph_ctx* ctx, const float* pos, uint32_t count, int layout, int memory) {
+    if (!ctx) return fail(PCISPH_ERR_INVALID_ARG, "ctx is NULL");
+    if (count && !pos) return fail(PCISPH_ERR_INVALID_ARG, "pos is NULL");
+    if (layout != PCISPH_LAYOUT_PACKED3 && layout != PCISPH_LAYOUT_FLOAT4)
+        return fail(PCISPH_ERR_INVALID_ARG, "positions take PACKED3 or FLOAT4");
+    if (count != ctx->params.boundary_count)
+        return fail(PCISPH_ERR_INCONSISTENT, "Inconsistent boundary_positions (" + std::to_string(count) + ") for " +
+                                                 std::to_string(ctx->params.boundary_count) + " particles");
+    DeviceGuard g(ctx->device);
+    uint32_t bk = ctx->params.fluid_count / 2;
+    bk -= bk % 64;
+    bk = std::max(64u, bk);
+    int rc = ctx->ensure_boundary(count, bk);
+    if (rc) return rc;
+    rc = ctx->copy_vectors_in(ctx->b_pos_in, pos, count, layout, memory);
+    if (rc) return rc;
+    if (memory == PCISPH_MEM_HOST) CUDA_TRY(cudaStreamSynchronize(ctx->stream()));
+    ctx->boundary_loaded = count;
+    ctx->boundary_updated = true;
+    return PCISPH_OK;
+}
+
+int pcisph_check_buffers_consistent(const pcisph_ctx* ctx) {
+    if (!ctx) return fail(PCISPH_ERR_INVALID_ARG, "ctx is NULL");
+    return ctx->check_consistent();
+}
+
+int pcisph_update(pcisph_ctx* ctx) {
+    if (!ctx) return fail(PCISPH_ERR_INVALID_ARG, "ctx is NULL");
+    DeviceGuard g(ctx->device);
+    return ctx->update();
+}
+
+int pcisph_step(pcisph_ctx* ctx, uint32_t steps) {
+    if (!ctx) return fail(PCISPH_ERR_INVALID_ARG, "ctx is NULL");
+    DeviceGuard g(ctx->device);
+    for (uint32_t i = 0; i < steps; ++i) {
+        int rc = ctx->update();
+        if (rc) return rc;
+    }
+    return PCISPH_OK;
+}
+
+int pcisph_sync(pcisph_ctx* ctx) {
+    if (!ctx) return fail(PCISPH_ERR_INVALID_ARG, "ctx is NULL");
+    DeviceGuard g(ctx->device);
+    CUDA_TRY(cudaStreamSynchronize(ctx->stream()));
+    return PCISPH_OK;
+}
+
+int pcisph_last_stats(pcisph_ctx* ctx, pcisph_step_stats* out) {
+    if (!ctx || !out) return fail(PCISPH_ERR_INVALID_ARG, "NULL argument");
+    DeviceGuard g(ctx->device);
+    return ctx->stats(out);
+}
+
+int pcisph_reset_stats(pcisph_ctx* ctx) {
+    if (!ctx) return fail(PCISPH_ERR_INVALID_ARG, "ctx is NULL");
+    DeviceGuard g(ctx->device);
+    CUDA_TRY(cudaStreamSynchronize(ctx->stream()));
+    Control zero{};
+    CUDA_TRY(cudaMemcpy(ctx->ctl, &zero, sizeof(Control), cudaMemcpyHostToDevice));
+    return PCISPH_OK;
+}
+
+int pcisph_get_field(pcisph_ctx* ctx, int field, void* dst, size_t dst_bytes, int layout, int memory) {
+    if (!ctx) return fail(PCISPH_ERR_INVALID_ARG, "ctx is NULL");
+    DeviceGuard g(ctx->device);
+    return ctx->get_field(field, dst, dst_bytes, layout, memory);
+}
+
+int pcisph_set_field(pcisph_ctx* ctx, int field, const void* src, size_t src_bytes, int layout, int memory) {
+    if (!ctx) return fail(PCISPH_ERR_INVALID_ARG, "ctx is NULL");
+    DeviceGuard g(ctx->device);
+    return ctx->set_field(field, src, src_bytes, layout, memory);
+}
+
+int pcisph_field_device_ptr(pcisph_ctx* ctx, int field, void** ptr, size_t* count, int* layout) {
+    if (!ctx || !ptr) return fail(PCISPH_ERR_INVALID_ARG, "NULL argument");
+    pcisph_ctx::FieldView v;
+    if (!ctx->field_view(field, &v)) return fail(PCISPH_ERR_INVALID_ARG, "unknown field");
+    *ptr = v.ptr;
+    if (count) *count = v.count;
+    if (layout) *layout = v.layout;
+    return PCISPH_OK;
+}
+
+int pcisph_run_stage(pcisph_ctx* ctx, int stage, int arg) {
+    if (!ctx) return fail(PCISPH_ERR_INVALID_ARG, "ctx is NULL");
+    DeviceGuard g(ctx->device);
+    return ctx->run_stage(stage, arg);
+}
+
+uint64_t pcisph_kernel_launches(const pcisph_ctx* ctx) {
+    if (!ctx) return 0;
+    // host-counted launches plus the corrective-loop kernels the device decided to run
+    DeviceGuard g(ctx->device);
+    cudaStreamSynchronize(ctx->stream());
+    Control h{};
+    cudaMemcpy(&h, ctx->ctl, sizeof(Control), cudaMemcpyDeviceToHost);
+    const uint64_t graph_iters = h.total_iters > ctx->host_mode_iters ? h.total_iters - ctx->host_mode_iters : 0;
+    return ctx->host_launches + graph_iters * (uint64_t)ctx->iter_launches;
+}
+
+int pcisph_profile_enable(pcisph_ctx* ctx, int enable) {
+    if (!ctx) return fail(PCISPH_ERR_INVALID_ARG, "ctx is NULL");
+    ctx->profiling = enable != 0;
+    if (enable) ctx->timings.clear();
+    return PCISPH_OK;
+}
+
+int pcisph_profile_read(pcisph_ctx* ctx, pcisph_kernel_time* out, int max_entries, int* n_entries) {
+    if (!ctx) return fail(PCISPH_ERR_INVALID_ARG, "ctx is NULL");
+    DeviceGuard g(ctx->device);
+    ctx->collect_timings();
+    int n = 0;
+    for (auto& kv : ctx->timings) {
+        if (out && n < max_entries) {
+            std::memset(out[n].name, 0, sizeof(out[n].name));
+            std::strncpy(out[n].name, kv.first.c_str(), sizeof(out[n].name) - 1);
+            out[n].launches = kv.second.launches;
+            out[n].total_ms = kv.second.ms;
+        }
+        ++n;
+    }
+    if (n_entries) *n_entries = n;
+    return PCISPH_OK;
+}
+
+int pcisph_hash_keys(const pcisph_sim_params* params, const float* pos, int layout, uint32_t count, uint32_t* keys,
+                     uint32_t* ids, void* stream) {
+    if (!params || (count && (!pos || !keys))) return fail(PCISPH_ERR_INVALID_ARG, "NULL argument");
+    if (params->bucket_count < 2) return fail(PCISPH_ERR_INVALID_ARG, "bucket_count must be >= 2");
+    if (layout != PCISPH_LAYOUT_PACKED3 && layout != PCISPH_LAYOUT_FLOAT4)
+        return fail(PCISPH_ERR_INVALID_ARG, "positions take PACKED3 or FLOAT4");
+    DevParams P{};
+    P.cell_size = params->cell_size;
+    P.bucket_count = params->bucket_count;
+    magic_for(params->bucket_count, &P.bk_magic, &P.bk_shift);
+    launch_hash(pos, layout == PCISPH_LAYOUT_PACKED3, count, P, keys, ids, static_cast<cudaStream_t>(stream));
+    CUDA_TRY(cudaGetLastError());
+    return PCISPH_OK;
+}
+
+struct pcisph_radixsort {
+    int device;
+    RadixSorter sorter;
+};
+
+int pcisph_radixsort_create(int device, pcisph_radixsort** out) {
+    if (!out) return fail(PCISPH_ERR_INVALID_ARG, "out is NULL");
+    DeviceGuard g(device);
+    CUDA_TRY(cudaFree(nullptr));
+    CUDA_TRY(radix_configure_kernels());
+    *out = new pcisph_radixsort{device, {}};
+    return PCISPH_OK;
+}
+
+void pcisph_radixsort_destroy(pcisph_radixsort* s) {
+    if (!s) return;
+    DeviceGuard g(s->device);
+    delete s;
+}
+
+int pcisph_radixsort_set_digit_bits(pcisph_radixsort* s, int bits) {
+    if (!s) return fail(PCISPH_ERR_INVALID_ARG, "sorter is NULL");
+    if (bits == 0) bits = 8;
+    if (bits < 4 || bits > 11) return fail(PCISPH_ERR_INVALID_ARG, "digit bits must be in 4..11");
+    s->sorter.set_digit_bits(bits);
+    return PCISPH_OK;
+}
+
+int pcisph_radixsort_enqueue(pcisph_radixsort* s, uint32_t* keys, uint32_t* values, size_t elements,
+                             unsigned int max_bits, void* stream) {
+    if (!s) return fail(PCISPH_ERR_INVALID_ARG, "sorter is NULL");
+    if (elements && (!keys || !values)) return fail(PCISPH_ERR_INVALID_ARG, "keys/values are NULL");
+    if (max_bits > 32) return fail(PCISPH_ERR_INVALID_ARG, "max_bits > 32");
+    DeviceGuard g(s->device);
+    cudaError_t e = s->sorter.sort(keys, values, elements, max_bits == 0 ? 32 : (int)max_bits, false,
+                                   static_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return fail(PCISPH_ERR_CUDA, std::string("radix sort: ") + cudaGetErrorString(e));
+    return PCISPH_OK;
+}
+
+}  // extern "C"

@@ -46,7 +46,8 @@ class Scene:
     boundary_pos: np.ndarray = field(default_factory=lambda: np.zeros((0, 3), np.float32))
     fluid_vel: np.ndarray = None           # (N, 3) float32 or None (zero)
     rest_density: float = 1000.0
-    viscosity: float = 0.2
+    viscosity: float = 0.2                 # dynamic viscosity mu (Pa s)
+    raw_viscosity: float = None            # the reference's viscosity_constant, if given directly
     surface_tension: float = 0.5
     gravity: float = -9.81
     threshold: float = 0.01
@@ -59,6 +60,19 @@ class Scene:
     @property
     def particle_radius(self):
         return 0.5 * self.spacing
+
+    def viscosity_constant(self):
+        """The reference's viscosity_constant for dynamic viscosity mu.
+
+        The reference's viscosity force is mu_c * m * sum_j (v_j - v_i)/rho_j * lap W
+        (PCISPH/data/kernels/pcisph.cl:146, :160); Mueller et al.'s (SCA 2003) is
+        (mu m / rho_i) * sum_j m (v_j - v_i)/rho_j * lap W. With rho_i = rho0 and
+        m = rho0 d^3 the two agree for mu_c = mu * m / rho0 = mu * d^3. (mu = 0.2 used
+        as mu_c directly makes the explicit viscosity unstable within a few steps.)
+        """
+        if self.raw_viscosity is not None:
+            return float(self.raw_viscosity)
+        return float(self.viscosity * self.spacing ** 3)
 
     @property
     def fluid_count(self):

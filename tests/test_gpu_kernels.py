@@ -1,0 +1,344 @@
+"""GPU parity: every CUDA kernel against the reference's own kernels (golden vectors) and the oracle.
+
+Integer results (cell keys, the stable permutation, cell ranges, reordered state) must be bit-exact. FP32
+fields computed by one kernel from identical inputs must agree within RTOL = 1e-5, normwise (see gpu_util).
+All calls go through the C ABI (libpcisph_gb300.so via ctypes).
+"""
+import numpy as np
+import pytest
+
+from gpu_util import RTOL, assert_close, fluid_like, kinetic_energy, params_from, rel_err
+from oracle.oracle import make_options
+from pcisph_gb300 import Fluid, RadixSort, hash_keys, scenes
+from pcisph_gb300._lib import ERR_INCONSISTENT, PcisphError, SimParams
+
+pytestmark = pytest.mark.gpu
+
+
+def _torch():
+    return pytest.importorskip("torch")
+
+
+def dev(a):
+    torch = _torch()
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+# ------------------------------------------------------------------------------------------------ hashing
+
+
+def test_hash_keys_bit_exact(golden):
+    torch = _torch()
+    g = golden("hash")
+    pos3 = g["pos"]
+    pos4 = np.concatenate([pos3, np.zeros((len(pos3), 1), np.float32)], 1)
+    for name in [k for k in g if k.startswith("keys_")]:
+        p = SimParams()
+        p.cell_size = float(g["cell"])
+        p.bucket_count = int(name[5:])
+        for arr in (pos3, pos4):
+            keys = torch.zeros(len(pos3), dtype=torch.int32, device="cuda")
+            ids = torch.zeros(len(pos3), dtype=torch.int32, device="cuda")
+            hash_keys(p, dev(arr), keys, ids)
+            torch.cuda.synchronize()
+            np.testing.assert_array_equal(keys.cpu().numpy().view(np.uint32), g[name], err_msg=name)
+            np.testing.assert_array_equal(ids.cpu().numpy(), np.arange(len(pos3)))
+
+
+# ----------------------------------------------------------------------------------------------- radix sort
+
+
+def _check_sort(rs, keys, vals, max_bits):
+    torch = _torch()
+    kd, vd = dev(keys.view(np.int32)), dev(vals.view(np.int32))
+    rs.enqueue(kd, vd, keys.size, max_bits=max_bits)
+    torch.cuda.synchronize()
+    order = np.argsort(keys, kind="stable")
+    np.testing.assert_array_equal(kd.cpu().numpy().view(np.uint32), keys[order])
+    np.testing.assert_array_equal(vd.cpu().numpy().view(np.uint32), vals[order])
+
+
+def test_radix_sort_golden(golden):
+    g = golden("sort")
+    rs = RadixSort(0)
+    i = 0
+    while f"keys_{i}" in g:
+        keys = g[f"keys_{i}"]
+        kd, vd = dev(keys.view(np.int32)), dev(np.arange(keys.size, dtype=np.int32))
+        rs.enqueue(kd, vd, keys.size, max_bits=0)
+        _torch().cuda.synchronize()
+        np.testing.assert_array_equal(kd.cpu().numpy().view(np.uint32), g[f"sorted_keys_{i}"])
+        np.testing.assert_array_equal(vd.cpu().numpy().view(np.uint32), g[f"sorted_vals_{i}"])
+        i += 1
+
+
+@pytest.mark.parametrize("digit_bits", [4, 5, 7, 8, 10, 11])
+def test_radix_sort_stable_random(digit_bits):
+    rng = np.random.default_rng(digit_bits)
+    rs = RadixSort(0, digit_bits=digit_bits)
+    for n, hi in [(1, 2), (63, 4), (64, 1 << 19), (65, 7), (4095, 1 << 19), (4096, 3), (4097, 1 << 22),
+                  ((1 << 20) + 1, 1 << 19), (300000, 1 << 32)]:
+        keys = rng.integers(0, hi, n, dtype=np.uint64).astype(np.uint32)
+        vals = rng.integers(0, 1 << 32, n, dtype=np.uint64).astype(np.uint32)
+        bits = 0 if hi == 1 << 32 else max(1, int(hi - 1).bit_length())
+        _check_sort(rs, keys, vals, bits)
+    # already sorted, reverse sorted, all equal (stability is visible in the values)
+    n = 100003
+    for keys in (np.arange(n, dtype=np.uint32), np.arange(n, dtype=np.uint32)[::-1].copy(),
+                 np.full(n, 5, np.uint32)):
+        _check_sort(rs, keys, np.arange(n, dtype=np.uint32), 17)
+
+
+# ------------------------------------------------------------------------------------ kernel chain vs golden
+
+
+def _load_case(golden, case, **kw):
+    g = golden(case)
+    p = params_from(g["params"])
+    f = fluid_like(p, **kw)
+    got = np.frombuffer(bytes(f.get_params()), np.int32).astype(np.int64)
+    want = np.frombuffer(bytes(p), np.int32).astype(np.int64)
+    assert np.all(np.abs(got - want) <= 1)  # derivation agrees with the reference (<= 1 ulp of libm)
+    f.set_fluid_state(g["f_pos0"], g["f_vel0"])
+    if p.boundary_count:
+        f.set_boundary_state(g["b_pos0"])
+    return g, p, f
+
+
+@pytest.mark.parametrize("case", ["step_boundary", "step_fluid"])
+def test_kernel_chain_vs_reference(golden, case):
+    g, p, f = _load_case(golden, case)
+    B = p.boundary_count
+    eq = np.testing.assert_array_equal
+    f.run_stage("sort")
+    eq(f.get_field("keys"), g["f_keys"])
+    eq(f.get_field("src"), g["f_src"])
+    eq(f.get_field("cell_offsets"), g["f_off"])
+    eq(f.get_field("sorted_position"), g["f_pos"])
+    eq(f.get_field("sorted_velocity"), g["f_vel"])
+    if B:
+        eq(f.get_field("boundary_keys"), g["b_keys"])
+        eq(f.get_field("boundary_src"), g["b_src"])
+        eq(f.get_field("boundary_cell_offsets"), g["b_off"])
+        eq(f.get_field("boundary_position"), g["b_pos"])
+        eq(f.get_field("boundary_init_density"), np.zeros(B, np.float32))
+    errs = {}
+    f.run_stage("density")
+    errs["density"] = assert_close("density", f.get_field("density"), g["rho"])
+    f.set_field("density", g["rho"])
+    f.run_stage("pack")
+    f.run_stage("normal")
+    errs["normal"] = assert_close("normal", f.get_field("normal"), g["normal"])
+    f.set_field("normal", g["normal"])
+    f.run_stage("force")
+    errs["other_force"] = assert_close("other_force", f.get_field("other_force"), g["f_other"])
+    eq(f.get_field("pressure"), np.zeros(p.fluid_count, np.float32))
+    errs["pred0"] = assert_close("pred0", f.get_field("predicted_position"), g["pred0"])
+    f.set_field("other_force", g["f_other"])
+    b_press = np.zeros(B, np.float32)
+    for it in range(2):
+        f.set_field("predicted_position", g[f"pred{it}"])
+        f.set_field("pressure", g[f"press_in{it}"])
+        if B:
+            f.set_field("boundary_pressure", b_press)
+            f.run_stage("boundary_pressure")
+            b_press = g[f"b_press{it}"]
+            errs[f"b_press{it}"] = assert_close("boundary_pressure", f.get_field("boundary_pressure"), b_press,
+                                                scale=p.density_variation_scaling_factor * p.rest_density)
+        f.run_stage("pressure")
+        # pressure and its variation cancel rho* - rho0: scale by the terms (rho0, delta * rho0)
+        errs[f"err{it}"] = assert_close("density_variation", f.get_field("density_variation"), g[f"err{it}"],
+                                        scale=p.rest_density)
+        errs[f"press{it}"] = assert_close("pressure", f.get_field("pressure"), g[f"press{it}"],
+                                          scale=p.density_variation_scaling_factor * p.rest_density * (it + 1))
+        f.set_field("pressure", g[f"press{it}"])
+        if B:
+            f.set_field("boundary_pressure", g[f"b_press{it}"])
+        f.run_stage("pack")
+        f.run_stage("pressure_force", 1 if it == 1 else 0)
+        errs[f"fpress{it}"] = assert_close("pressure_force", f.get_field("pressure_force"), g[f"fpress{it}"])
+        if it == 0:
+            errs["pred1"] = assert_close("pred1", f.get_field("predicted_position"), g["pred1"])
+        else:
+            errs["x_new"] = assert_close("x_new", f.get_field("position"), g["x_new"])
+            errs["v_new"] = assert_close("v_new", f.get_field("velocity"), g["v_new"])
+    print(case, {k: f"{v:.1e}" for k, v in errs.items()})
+
+
+def test_boundary_self_density_computed(golden):
+    g, p, f = _load_case(golden, "step_boundary", boundary_self_density=1)
+    f.run_stage("sort")
+    assert_close("boundary_init_density", f.get_field("boundary_init_density"), g["b_init"])
+    f.run_stage("density")
+    f.run_stage("normal")
+    f.run_stage("force")
+    for it in range(2):
+        f.set_field("predicted_position", g[f"pred{it}"])
+        f.set_field("boundary_pressure", np.zeros(p.boundary_count, np.float32))
+        f.run_stage("boundary_pressure")
+        assert_close("boundary_pressure", f.get_field("boundary_pressure"), g[f"b_press_computed{it}_from0"],
+                     scale=p.density_variation_scaling_factor * p.rest_density)
+
+
+@pytest.mark.parametrize("case", ["step_boundary", "step_fluid"])
+@pytest.mark.parametrize("loop_mode", [0, 1])
+def test_full_steps_vs_reference(golden, case, loop_mode):
+    """Fluid::update sequence (min 3 / max 7 iterations, no walls) against the reference's full steps."""
+    g, p, f = _load_case(golden, case, loop_mode=loop_mode)
+    k = 0
+    while f"step{k}_iters" in g:
+        f.update()
+        st = f.stats()
+        assert st.iterations == int(g[f"step{k}_iters"]), (k, st.iterations)
+        if k == 0:
+            np.testing.assert_array_equal(f.get_field("src"), g["step0_f_src"])
+            assert_close("density", f.get_field("density"), g["step0_f_rho"])
+            assert_close("normal", f.get_field("normal"), g["step0_f_normal"])
+            assert_close("other_force", f.get_field("other_force"), g["step0_f_other"])
+        # after k corrective iterations the fields carry the loop's conditioning; positions stay within 1e-5
+        # of the box scale, velocities within 1e-3 of their scale (measured GPU-vs-FP64 error bounds these)
+        assert_close("position", f.get_field("position"), g[f"step{k}_f_pos"])
+        assert_close("velocity", f.get_field("velocity"), g[f"step{k}_f_vel"], rtol=1e-3)
+        k += 1
+
+
+def test_graph_and_host_loop_identical():
+    sc = scenes.small_dam(10, seed=3)
+    out = []
+    for mode in (0, 1):
+        f = Fluid(0)
+        from pcisph_gb300 import setup_scene
+        setup_scene(f, sc, loop_mode=mode)
+        f.step(5)
+        st = f.stats()
+        out.append((f.get_field("position"), f.get_field("velocity"), f.get_field("pressure"), st.total_iterations))
+    for a, b in zip(out[0][:3], out[1][:3]):
+        np.testing.assert_array_equal(a, b)
+    assert out[0][3] == out[1][3]
+
+
+# ------------------------------------------------------------------------------------------- full step vs FP64
+
+
+def test_full_step_error_vs_fp64(oracle):
+    """One step (fixed 4 iterations, walls on) from identical state: the GPU's error against the FP64 rerun
+    is of the order of the FP32 oracle's own error against it."""
+    sc = scenes.small_dam(12, seed=4)
+    rng = np.random.default_rng(4)
+    vel = (rng.standard_normal((sc.fluid_count, 3)) * 0.05).astype(np.float32)
+    p = oracle.derive_params(sc.particle_radius, sc.rest_density, sc.fluid_count, 0, sc.delta_t, sc.gravity,
+                             sc.viscosity_constant(), sc.surface_tension)
+    opts = make_options(threshold=0.01, min_iters=4, max_iters=4, walls=True, box_hi=sc.box_hi)
+    s32 = oracle.new_state(p, sc.fluid_pos, vel)
+    s64 = oracle.new_state(p, sc.fluid_pos, vel, dtype=np.float64)
+    oracle.step(p, opts, s32)
+    oracle.step(p, opts, s64)
+    f = fluid_like(p, min_iters=4, max_iters=4, walls=True, box_hi=sc.box_hi)
+    f.set_fluid_state(sc.fluid_pos, vel)
+    f.update()
+    assert f.stats().iterations == 4
+    np.testing.assert_array_equal(f.get_field("src"), s64["f_src"])
+    report = {}
+    for name, key in [("density", "f_rho"), ("normal", "f_normal"), ("other_force", "f_other"),
+                      ("pressure", "f_press"), ("pressure_force", "f_fpress"), ("position", "f_pos"),
+                      ("velocity", "f_vel")]:
+        e_gpu = rel_err(f.get_field(name), s64[key])
+        e_cpu = rel_err(s32[key], s64[key])
+        report[name] = (e_gpu, e_cpu)
+        assert e_gpu <= 10 * e_cpu + 1e-6, (name, e_gpu, e_cpu)
+    print({k: f"gpu {a:.1e} / fp32 oracle {b:.1e}" for k, (a, b) in report.items()})
+
+
+def test_long_run_statistics_vs_oracle(oracle):
+    """200 steps of a small dam break: trajectories diverge (chaos), statistics must not."""
+    sc = scenes.small_dam(12, seed=5)
+    p = oracle.derive_params(sc.particle_radius, sc.rest_density, sc.fluid_count, 0, sc.delta_t, sc.gravity,
+                             sc.viscosity_constant(), sc.surface_tension)
+    opts = make_options(threshold=0.01, min_iters=3, max_iters=50, walls=True, box_hi=sc.box_hi)
+    s = oracle.new_state(p, sc.fluid_pos, np.zeros((sc.fluid_count, 3)))
+    f = fluid_like(p, min_iters=3, max_iters=50, walls=True, box_hi=sc.box_hi)
+    f.set_fluid_state(sc.fluid_pos, None)
+    ke_o, ke_g, com_o, com_g, it_o, it_g = [], [], [], [], [], []
+    for k in range(200):
+        st_o = oracle.step(p, opts, s)
+        f.update()
+        st_g = f.stats()
+        assert st_o.max_err / p.rest_density < 0.01 and st_g.max_density_error < 0.01
+        it_o.append(st_o.iterations)
+        it_g.append(st_g.iterations)
+        if k % 10 == 9:
+            ke_o.append(kinetic_energy(p.particle_mass, s["f_vel"]))
+            ke_g.append(kinetic_energy(p.particle_mass, f.get_field("velocity")))
+            com_o.append(s["f_pos"].astype(np.float64).mean(0))
+            com_g.append(f.get_field("position").astype(np.float64).mean(0))
+    ke_o, ke_g = np.array(ke_o), np.array(ke_g)
+    com_o, com_g = np.array(com_o), np.array(com_g)
+    ke_rel = np.abs(ke_g - ke_o).max() / ke_o.max()
+    com_abs = np.abs(com_g - com_o).max()
+    print(f"KE rel diff {ke_rel:.2e}, COM abs diff {com_abs:.2e} m, mean iters gpu {np.mean(it_g):.3f} "
+          f"oracle {np.mean(it_o):.3f}")
+    assert ke_rel < 0.02
+    assert com_abs < 2e-3
+    assert abs(np.mean(it_g) - np.mean(it_o)) < 0.5
+
+
+# ------------------------------------------------------------------------------------------------ edge cases
+
+
+def test_inconsistent_state_is_an_error():
+    f = Fluid(0)
+    f.set_particle_radius(0.01)
+    f.set_fluid_count(100)
+    with pytest.raises(PcisphError) as e:
+        f.update()
+    assert e.value.code == ERR_INCONSISTENT and "Inconsistent positions_size" in str(e.value)
+    with pytest.raises(PcisphError):
+        f.set_fluid_state(np.zeros((99, 3), np.float32))
+
+
+def test_zero_particles_is_a_no_op():
+    f = Fluid(0)
+    f.set_particle_radius(0.01)
+    f.set_fluid_count(0)
+    f.update()
+
+
+def test_single_particle_step():
+    f = Fluid(0)
+    f.set_particle_radius(0.01)
+    f.set_rest_density(1000)
+    f.set_delta_t(1e-3)
+    f.set_gravity(-9.81)
+    f.set_fluid_count(1)
+    f.prepare()
+    f.set_fluid_state(np.array([[0.5, 0.5, 0.5]], np.float32))
+    f.update()
+    v = f.get_field("velocity")
+    np.testing.assert_allclose(v, [[0.0, -9.81e-3, 0.0]], rtol=1e-6)
+
+
+def test_nonfinite_state_is_flagged():
+    sc = scenes.small_dam(6)
+    pos = sc.fluid_pos.copy()
+    pos[7] = np.nan
+    f = Fluid(0)
+    from pcisph_gb300 import setup_scene
+    setup_scene(f, sc)
+    f.set_fluid_state(pos)
+    f.update()
+    assert f.stats().status & 2
+
+
+def test_setters_zero_velocities_like_the_reference():
+    """A parameter change re-derives on the next update and zeroes the velocities (Fluid.cpp:461-463)."""
+    from pcisph_gb300 import setup_scene
+    sc = scenes.small_dam(6)
+    out = []
+    for v0 in (np.ones((sc.fluid_count, 3), np.float32), None):
+        f = Fluid(0)
+        setup_scene(f, sc)
+        f.set_fluid_state(sc.fluid_pos, v0)
+        f.set_gravity(-1.0)
+        f.update()
+        out.append(f.get_field("velocity"))
+    np.testing.assert_array_equal(out[0], out[1])
