@@ -1,0 +1,318 @@
+"""Benchmark of the PCISPH time step on GB300: particle-steps/s at 1,048,576 particles.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+One JSON line on stdout (rank 0). The workload is the 1M-particle dam break: a 128 x 128 x 64 jittered
+lattice (d = 0.005 m, h = 0.01 m, m = rho0 d^3), dt = 2.5e-4 s, rho0 = 1000, mu = 0.2 Pa s,
+gamma = 0.5, g = -9.81, reflecting walls (restitution 0.5) in [0,1.6]x[0,1.2]x[0,0.8] m, 3..50 corrective
+iterations until the max density error is below 1%. A "step" is one full PCISPH time step.
+
+  value     N x K / sum of the K steps' device times (CUDA events on the step's stream), state resident in
+            HBM, a 256 MB buffer written between timed steps (L2 flush, not timed)
+  e2e       the same metric through the C ABI with pinned host buffers: each step uploads positions and
+            velocities, steps, and reads both back
+  roofline  the dominant kernel (largest share of a per-kernel CUDA-event pass over the same state)
+  cpu_baseline  the oracle (CPU port of the reference step) on all host cores, from the same state
+  --impl reference  the reference's CPU implementation (the oracle port; the OpenCL runtime the reference
+            needs does not exist on these machines) timed on the host cores on the same workload
+With --gpus N > 1 (torchrun) every rank runs its own replica (the step does not shard); value is summed.
+"""
+import argparse
+import json
+import os
+import signal
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+# algorithmic bytes per particle per launch (12 B per 3-vector, 4 B per scalar, the cell table amortised
+# at 4 B per particle): compulsory reads and writes of each fused kernel
+ALGO_BYTES = {
+    "density": 20,          # x 12 + cell table 4 + rho 4
+    "normal": 32,           # x 12 + rho 4 + cell table 4 + n 12
+    "force": 72,            # x, v, n 36 + rho 4 + cell table 4 + F_o 12 + p 4 + x* 12
+    "pressure": 40,         # x 12 + x* 12 + p 4 + cell table 4 + p 4 + err 4
+    "pressure_force": 72,   # x 12 + p 4 + rho 4 + cell table 4 + F_p 12; predict: v 12, F_o 12, x* 12
+    "reorder": 60,          # keys 4 + ids 4 + x, v gathered 24 + x, v written 24 + table 4
+    "hash": 20,             # x 12 + key 4 + id 4
+    "radix_sort": 48,       # 3 passes of 8 B read + 8 B written
+}
+WORKLOAD = ("dam break 128x128x64 = 1,048,576 particles, d=0.005 m, dt=2.5e-4 s, reflecting walls, "
+            "3-50 corrective iterations to <1% density error")
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--cpu-seconds", type=float, default=20.0, help="bound of the CPU baseline sample")
+    return ap.parse_args()
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def ncu_traffic():
+    """Per-kernel DRAM bytes per particle from the committed ncu summary (profiles/ncu_traffic.txt)."""
+    out = {}
+    path = os.path.join(ROOT, "profiles", "ncu_traffic.txt")
+    if not os.path.exists(path):
+        return out
+    with open(path) as f:
+        for line in f:
+            if line.startswith("kernel="):
+                kv = dict(tok.split("=", 1) for tok in line.split())
+                out[kv["kernel"]] = float(kv["dram_bytes_per_particle"])
+    return out
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms while the benchmark runs."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.proc, self.path, self.gpu = None, None, gpu
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.send_signal(signal.SIGTERM)
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = []
+        with open(self.path) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({n for r in rows for n, v in zip(names, r[5:9]) if v.lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": float(rows[0][2]) if rows[0][2].replace(".", "").isdigit() else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def cpu_step_rate(scene, pos, vel, seconds, max_steps=None):
+    """Oracle steps from (pos, vel) until `seconds` of step time; returns (particle-steps/s, steps, iters)."""
+    import numpy as np
+
+    from oracle.oracle import get as get_oracle
+    from oracle.oracle import make_options
+    O = get_oracle()
+    p = O.derive_params(scene.particle_radius, scene.rest_density, scene.fluid_count, 0, scene.delta_t,
+                        scene.gravity, scene.viscosity_constant(), scene.surface_tension)
+    opts = make_options(threshold=scene.threshold, min_iters=scene.min_iters, max_iters=scene.max_iters,
+                        walls=scene.walls, box_lo=scene.box_lo, box_hi=scene.box_hi, restitution=scene.restitution)
+    s = O.new_state(p, pos, vel)
+    t_total, steps, iters = 0.0, 0, []
+    while t_total < seconds and (max_steps is None or steps < max_steps):
+        t0 = time.perf_counter()
+        st = O.step(p, opts, s)
+        t_total += time.perf_counter() - t0
+        steps += 1
+        iters.append(st.iterations)
+    return scene.fluid_count * steps / t_total, steps, float(np.mean(iters)), s
+
+
+def reference_arm(args, rank, world):
+    """The reference's CPU implementation of the step (the oracle port) on all host cores."""
+    if rank != 0:
+        return
+    from pcisph_gb300 import scenes
+    import numpy as np
+    sc = scenes.config1()
+    pos, vel = sc.fluid_pos, np.zeros_like(sc.fluid_pos)
+    w = min(args.warmup, 3)
+    if w:
+        _, _, _, s = cpu_step_rate(sc, pos, vel, float("inf"), max_steps=w)
+        pos, vel = s["f_pos"], s["f_vel"]
+    rate, steps, iters, _ = cpu_step_rate(sc, pos, vel, args.cpu_seconds * 2, max_steps=args.steps)
+    cores = os.cpu_count()
+    line = {
+        "impl": "reference", "metric": "particle-steps/s @1M (<=1% rho err)", "value": rate,
+        "unit": "particle-steps/s", "n_gpus": 0, "steps": steps, "warmup": w, "ms_per_step": 1e3 * sc.fluid_count / rate,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded jittered lattice)",
+        "config": {"workload": WORKLOAD, "particles": sc.fluid_count, "mean_iterations": iters},
+        "cpu_baseline": {"value": rate, "unit": "particle-steps/s", "cores": cores, "kind": "port",
+                         "sample": f"{sc.fluid_count} particles x {steps} steps after {w} warm-up steps "
+                                   f"(oracle/pcisph_oracle.cpp, OpenMP over particles; the reference's OpenCL "
+                                   f"runtime is unavailable on this box)"},
+        "e2e": {"value": rate, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        reference_arm(args, rank, world)
+        return
+    import numpy as np
+    import torch
+    import torch.distributed as dist
+
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    from pcisph_gb300 import Fluid, build, scenes, setup_scene
+    build.build()
+    sc = scenes.config1()
+    N = sc.fluid_count
+    stream = torch.cuda.Stream()  # a real stream: the library launches on it, the events are recorded on it
+    torch.cuda.set_stream(stream)
+    f = Fluid(local, stream=stream.cuda_stream)
+    setup_scene(f, sc)
+    sampler = ClockSampler(local)
+    sampler.start()
+    for _ in range(args.warmup):
+        f.update()
+    torch.cuda.synchronize()
+    # snapshot of the state after warm-up: the profile pass, the e2e pass and the CPU baseline replay the
+    # same steps as the timed loop (the step is deterministic)
+    snap_pos = torch.empty((N, 4), dtype=torch.float32, device="cuda")
+    snap_vel = torch.empty((N, 4), dtype=torch.float32, device="cuda")
+    f.get_field("position", layout="float4", out=snap_pos)
+    f.get_field("velocity", layout="float4", out=snap_vel)
+    f.reset_stats()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    st0 = f.stats()
+    launches0 = f.kernel_launches()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    wall0 = time.perf_counter()
+    max_err = 0.0
+    for k in range(args.steps):
+        flush.fill_(k & 0xFF)
+        starts[k].record(stream)
+        f.update()
+        ends[k].record(stream)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - wall0
+    if world > 1:
+        dist.barrier()
+    st1 = f.stats()
+    launches = f.kernel_launches() - launches0
+    step_ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
+    total_ms = sum(step_ms)
+    if world > 1:
+        t = torch.tensor([total_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    iters = (st1.total_iterations - st0.total_iterations) / max(1, st1.steps - st0.steps)
+    status_bits = st1.status_all
+    value = N * args.steps * world / (total_ms / 1e3)
+
+    # per-kernel CUDA events over the first steps of the timed loop again (host-driven loop, same kernels)
+    prof_steps = min(args.steps, 20)
+    f.set_fluid_state(snap_pos, snap_vel)
+    f.profile(True)
+    f.step(prof_steps)
+    prof = f.profile_read()
+    f.profile(False)
+    clocks = sampler.stop()
+    tot = sum(ms for _, ms in prof.values())
+    dom = max(prof.items(), key=lambda kv: kv[1][1])
+    dname, (dl, dms) = dom
+    avg_s = dms / dl / 1e3
+    peak, peak_kind = peaks()
+    achieved = ALGO_BYTES.get(dname, 0) * N / avg_s / 1e9
+    traffic = ncu_traffic().get(dname)
+    kernels = {k: {"launches": l, "avg_us": 1e3 * ms / l, "share": ms / tot,
+                   "algo_GBps": ALGO_BYTES.get(k, 0) * N / (ms / l / 1e3) / 1e9} for k, (l, ms) in prof.items()}
+
+    # e2e through the C ABI with pinned host buffers, over the same first steps
+    pos_h = torch.empty((N, 3), dtype=torch.float32, pin_memory=True).numpy()
+    vel_h = torch.empty((N, 3), dtype=torch.float32, pin_memory=True).numpy()
+    f.set_fluid_state(snap_pos, snap_vel)
+    f.get_field("position", out=pos_h)
+    f.get_field("velocity", out=vel_h)
+    start_pos, start_vel = pos_h.copy(), vel_h.copy()
+    e2e_steps = prof_steps
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        f.set_fluid_state(pos_h, vel_h)
+        f.update()
+        f.get_field("position", out=pos_h)
+        f.get_field("velocity", out=vel_h)
+    e2e_s = time.perf_counter() - t0
+    e2e = {"value": N * e2e_steps * world / e2e_s, "unit": "particle-steps/s", "h2d_bytes_per_step": 24 * N,
+           "d2h_bytes_per_step": 24 * N, "steps": e2e_steps,
+           "device_value_same_steps": N * e2e_steps * world / (sum(step_ms[:e2e_steps]) / 1e3)}
+
+    cpu = None
+    if rank == 0 and world == 1:
+        rate, csteps, citers, _ = cpu_step_rate(sc, start_pos, start_vel, args.cpu_seconds)
+        cpu = {"value": rate, "unit": "particle-steps/s", "cores": os.cpu_count(), "kind": "port",
+               "sample": f"{N} particles x the first {csteps} of the timed steps, from the same state "
+                         f"(mean {citers:.2f} corrective iterations), oracle/pcisph_oracle.cpp with OpenMP"}
+    if rank == 0:
+        line = {
+            "metric": "particle-steps/s @1M (<=1% rho err)", "value": value, "unit": "particle-steps/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded jittered lattice)",
+            "config": {"workload": WORKLOAD, "particles": N, "parallelism": f"replicas x{world}",
+                       "mean_iterations": iters, "max_density_error_last": st1.max_density_error,
+                       "step_ms_min_median_max": [min(step_ms), statistics.median(step_ms), max(step_ms)],
+                       "converged_all_steps": (status_bits & 1) == 0, "status_bits": status_bits,
+                       "l2": "256 MB written between timed steps (not timed); step working set ~200 MB > L2",
+                       "wall_s_timed_loop": wall},
+            "e2e": e2e,
+            "gpu_launches": launches,
+            "roofline": {"bound": "hbm", "kernel": dname, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_kind": peak_kind,
+                         "traffic": traffic * N if traffic else None,
+                         "algo_bytes_per_particle": ALGO_BYTES.get(dname, 0), "avg_launch_us": avg_s * 1e6},
+            "kernels": kernels,
+            "cpu_baseline": cpu,
+            "clocks": clocks,
+        }
+        print(json.dumps(line), flush=True)
+    f.close()
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -88,6 +88,8 @@ typedef struct pcisph_options {
     int32_t loop_mode;             /* default 0: the corrective loop is decided on the device (CUDA graph with
                                       a conditional while node); 1: host reads the decision each iteration,
                                       like the reference (Fluid.cpp:300-306) */
+    int32_t kernel_variant;        /* default 0: neighbour sweeps with one warp per bucket run and shared-memory
+                                      staging; 1: one thread per particle walking the 27 buckets */
 } pcisph_options;
 
 typedef struct pcisph_step_stats {

@@ -49,7 +49,7 @@ class SimParams(C.Structure):
 class Options(C.Structure):
     _fields_ = [("min_iterations", C.c_int32), ("max_iterations", C.c_int32), ("walls", C.c_int32),
                 ("box_lo", C.c_float * 3), ("box_hi", C.c_float * 3), ("restitution", C.c_float),
-                ("boundary_self_density", C.c_int32), ("loop_mode", C.c_int32)]
+                ("boundary_self_density", C.c_int32), ("loop_mode", C.c_int32), ("kernel_variant", C.c_int32)]
 
 
 class StepStats(C.Structure):

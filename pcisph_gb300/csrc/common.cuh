@@ -40,6 +40,7 @@ struct Control {
     unsigned long long steps;
     unsigned long long total_iters;
     unsigned int guard_iters;    // loop iterations counted by the pressure-force kernel (bounds the graph loop)
+    unsigned int n_groups;       // bucket runs listed by the reorder kernel this step
 };
 
 __host__ __device__ inline void magic_for(uint32_t d, uint32_t* magic, uint32_t* shift) {

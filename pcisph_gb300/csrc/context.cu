@@ -25,6 +25,7 @@
 #include "common.cuh"
 #include "radix_sort.cuh"
 #include "step_kernels.cuh"
+#include "sweep.cuh"
 
 using namespace pcisph;
 
@@ -148,11 +149,11 @@ struct Carver {
 };
 
 size_t fluid_arena_bytes(uint32_t n, uint32_t bk) {
-    return 10 * align256((size_t)n * 16) + 3 * align256((size_t)n * 4) + 2 * align256((size_t)n * 4) +
+    return 10 * align256((size_t)n * 16) + 3 * align256((size_t)n * 4) + 4 * align256((size_t)n * 4) +
            align256((size_t)bk * 8);
 }
 size_t boundary_arena_bytes(uint32_t n, uint32_t bk) {
-    return 3 * align256((size_t)n * 16) + 4 * align256((size_t)n * 4) + align256((size_t)bk * 8);
+    return 3 * align256((size_t)n * 16) + 5 * align256((size_t)n * 4) + align256((size_t)bk * 8);
 }
 
 struct KernelTiming {
@@ -183,6 +184,12 @@ struct pcisph_ctx {
     Control* host_ctl = nullptr;  // pinned
     RadixSorter sorter;
     DevParams P{};
+    SweepGrid sweep_grid{};
+
+    SweepArgs sweep_args() const {
+        return SweepArgs{b.groups, &b.ctl->n_groups, sorted_keys, b.cells, b.b_cells, b.codes, b.b_codes};
+    }
+    bool warp_sweeps() const { return opts.kernel_variant == 0; }
 
     cudaGraphExec_t graph_exec = nullptr;
     bool graph_valid = false;
@@ -227,6 +234,8 @@ struct pcisph_ctx {
         b.err = c.take<float>(n);
         f_keys = c.take<uint32_t>(n);
         f_ids = c.take<uint32_t>(n);
+        b.codes = c.take<uint32_t>(n);
+        b.groups = c.take<uint32_t>(n);
         b.cells = c.take<uint2>(bk);
         CUDA_TRY(cudaMemsetAsync(fluid_block.p, 0, fluid_arena_bytes(n, bk), stream()));
         fluid_cap_n = n;
@@ -250,6 +259,7 @@ struct pcisph_ctx {
         b.b_init = c.take<float>(n);
         b_keys = c.take<uint32_t>(n);
         b_ids = c.take<uint32_t>(n);
+        b.b_codes = c.take<uint32_t>(n);
         b.b_cells = c.take<uint2>(bk);
         CUDA_TRY(cudaMemsetAsync(boundary_block.p, 0, boundary_arena_bytes(n, bk), stream()));
         boundary_cap_n = n;
@@ -386,7 +396,7 @@ struct pcisph_ctx {
             CUDA_TRY(cudaMemcpyAsync(b_ids, sv, (size_t)B * 4, cudaMemcpyDeviceToDevice, s));
         }
         timed("reorder_boundary", s,
-              [&] { launch_reorder(b_keys, b_ids, b_pos_in, nullptr, B, b.b_pos, nullptr, b.b_cells, params.bucket_count, b.ctl, s); });
+              [&] { launch_reorder(b_keys, b_ids, b_pos_in, nullptr, B, b.b_pos, nullptr, b.b_cells, b.b_codes, nullptr, P, b.ctl, s); });
         if (opts.boundary_self_density) timed("boundary_self_density", s, [&] { launch_boundary_self_density(P, b, s); });
         else CUDA_TRY(cudaMemsetAsync(b.b_init, 0, (size_t)B * 4, s));
         host_launches += nl + 1 + (opts.boundary_self_density ? 1 : 0);
@@ -409,11 +419,18 @@ struct pcisph_ctx {
         nl += r;
         sorted_keys = sk;
         sorted_ids = sv;
-        timed("reorder", s, [&] { launch_reorder(sk, sv, b.state_pos, b.state_vel, N, b.pos, b.vel, b.cells, params.bucket_count, b.ctl, s); });
-        timed("density", s, [&] { launch_density(P, b, s); });
-        timed("normal", s, [&] { launch_normal(P, b, s); });
+        timed("reorder", s, [&] { launch_reorder(sk, sv, b.state_pos, b.state_vel, N, b.pos, b.vel, b.cells, b.codes, b.groups, P, b.ctl, s); });
+        const SweepArgs A = sweep_args();
+        if (warp_sweeps()) {
+            timed("density", s, [&] { launch_density_sweep(P, b, A, sweep_grid, s); });
+            timed("normal", s, [&] { launch_normal_sweep(P, b, A, sweep_grid, s); });
+        } else {
+            timed("density", s, [&] { launch_density(P, b, s); });
+            timed("normal", s, [&] { launch_normal(P, b, s); });
+        }
         if (B && cudaMemsetAsync(b.b_press, 0, (size_t)B * 4, s) != cudaSuccess) return -1;
-        timed("force", s, [&] { launch_force(P, b, s); });
+        if (warp_sweeps()) timed("force", s, [&] { launch_force_sweep(P, b, A, sweep_grid, s); });
+        else timed("force", s, [&] { launch_force(P, b, s); });
         nl += 4;
         if (cudaGetLastError() != cudaSuccess) return -1;
         return nl;
@@ -425,8 +442,14 @@ struct pcisph_ctx {
             timed("boundary_pressure", s, [&] { launch_boundary_pressure(P, b, s); });
             ++nl;
         }
-        timed("pressure", s, [&] { launch_pressure(P, b, s); });
-        timed("pressure_force", s, [&] { launch_pressure_force(P, b, 0, cond, use_cond, s); });
+        if (warp_sweeps()) {
+            const SweepArgs A = sweep_args();
+            timed("pressure", s, [&] { launch_pressure_sweep(P, b, A, sweep_grid, s); });
+            timed("pressure_force", s, [&] { launch_pressure_force_sweep(P, b, A, sweep_grid, 0, cond, use_cond, s); });
+        } else {
+            timed("pressure", s, [&] { launch_pressure(P, b, s); });
+            timed("pressure_force", s, [&] { launch_pressure_force(P, b, 0, cond, use_cond, s); });
+        }
         nl += 2;
         return nl;
     }
@@ -558,16 +581,36 @@ struct pcisph_ctx {
                 if (nl < 0) return PCISPH_ERR_CUDA;
                 sorted_keys = sk;
                 sorted_ids = sv;
-                launch_reorder(sk, sv, b.state_pos, b.state_vel, N, b.pos, b.vel, b.cells, params.bucket_count, b.ctl, s);
+                launch_reorder(sk, sv, b.state_pos, b.state_vel, N, b.pos, b.vel, b.cells, b.codes, b.groups, P, b.ctl, s);
                 host_launches += nl + 2;
                 break;
             }
-            case PCISPH_STAGE_DENSITY: launch_density(P, b, s); ++host_launches; break;
-            case PCISPH_STAGE_NORMAL: launch_normal(P, b, s); ++host_launches; break;
-            case PCISPH_STAGE_FORCE: launch_force(P, b, s); ++host_launches; break;
+            case PCISPH_STAGE_DENSITY:
+                if (warp_sweeps()) launch_density_sweep(P, b, sweep_args(), sweep_grid, s);
+                else launch_density(P, b, s);
+                ++host_launches;
+                break;
+            case PCISPH_STAGE_NORMAL:
+                if (warp_sweeps()) launch_normal_sweep(P, b, sweep_args(), sweep_grid, s);
+                else launch_normal(P, b, s);
+                ++host_launches;
+                break;
+            case PCISPH_STAGE_FORCE:
+                if (warp_sweeps()) launch_force_sweep(P, b, sweep_args(), sweep_grid, s);
+                else launch_force(P, b, s);
+                ++host_launches;
+                break;
             case PCISPH_STAGE_BOUNDARY_PRESSURE: launch_boundary_pressure(P, b, s); ++host_launches; break;
-            case PCISPH_STAGE_PRESSURE: launch_pressure(P, b, s); ++host_launches; break;
-            case PCISPH_STAGE_PRESSURE_FORCE: launch_pressure_force(P, b, arg ? 2 : 1, 0, false, s); ++host_launches; break;
+            case PCISPH_STAGE_PRESSURE:
+                if (warp_sweeps()) launch_pressure_sweep(P, b, sweep_args(), sweep_grid, s);
+                else launch_pressure(P, b, s);
+                ++host_launches;
+                break;
+            case PCISPH_STAGE_PRESSURE_FORCE:
+                if (warp_sweeps()) launch_pressure_force_sweep(P, b, sweep_args(), sweep_grid, arg ? 2 : 1, 0, false, s);
+                else launch_pressure_force(P, b, arg ? 2 : 1, 0, false, s);
+                ++host_launches;
+                break;
             case PCISPH_STAGE_PACK: launch_pack(P, b, s); ++host_launches; break;
             case PCISPH_STAGE_BOUNDARY_PRESSURE_RESET:
                 if (params.boundary_count) CUDA_TRY(cudaMemsetAsync(b.b_press, 0, (size_t)params.boundary_count * 4, s));
@@ -758,8 +801,11 @@ int pcisph_create(int device, void* stream, pcisph_ctx** out) {
     DeviceGuard g(device);
     CUDA_TRY(cudaFree(nullptr));  // create the primary context
     CUDA_TRY(radix_configure_kernels());
+    SweepGrid sg{};
+    CUDA_TRY(sweep_configure(&sg));
     pcisph_ctx* c = new pcisph_ctx();
     c->device = device;
+    c->sweep_grid = sg;
     pcisph_default_options(&c->opts);
     c->params.rest_density = 1000.f;
     cudaError_t e = cudaStreamCreateWithFlags(&c->capture_stream, cudaStreamNonBlocking);
@@ -817,6 +863,8 @@ int pcisph_set_options(pcisph_ctx* ctx, const pcisph_options* o) {
     if (o->max_iterations < 1 || o->min_iterations < 1 || o->max_iterations > 10000)
         return fail(PCISPH_ERR_INVALID_ARG, "iteration limits must be in 1..10000");
     if (o->loop_mode != 0 && o->loop_mode != 1) return fail(PCISPH_ERR_INVALID_ARG, "loop_mode must be 0 or 1");
+    if (o->kernel_variant != 0 && o->kernel_variant != 1)
+        return fail(PCISPH_ERR_INVALID_ARG, "kernel_variant must be 0 or 1");
     const bool bsd_changed = o->boundary_self_density != ctx->opts.boundary_self_density;
     ctx->opts = *o;
     if (bsd_changed) ctx->boundary_updated = true;
@@ -928,6 +976,12 @@ int pcisph_reset_stats(pcisph_ctx* ctx) {
     if (!ctx) return fail(PCISPH_ERR_INVALID_ARG, "ctx is NULL");
     DeviceGuard g(ctx->device);
     CUDA_TRY(cudaStreamSynchronize(ctx->stream()));
+    Control h{};
+    CUDA_TRY(cudaMemcpy(&h, ctx->ctl, sizeof(Control), cudaMemcpyDeviceToHost));
+    // keep the launch count: fold the device-decided loop launches into the host count
+    const uint64_t graph_iters = h.total_iters > ctx->host_mode_iters ? h.total_iters - ctx->host_mode_iters : 0;
+    ctx->host_launches += graph_iters * (uint64_t)ctx->iter_launches;
+    ctx->host_mode_iters = 0;
     Control zero{};
     CUDA_TRY(cudaMemcpy(ctx->ctl, &zero, sizeof(Control), cudaMemcpyHostToDevice));
     return PCISPH_OK;

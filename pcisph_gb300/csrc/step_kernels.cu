@@ -15,6 +15,7 @@
 //   pressure force then predicts for the next iteration, or integrates (with
 //                  optional walls) when the loop has stopped
 #include "step_kernels.cuh"
+#include "sweep.cuh"
 
 namespace pcisph {
 namespace {
@@ -42,25 +43,45 @@ __global__ void __launch_bounds__(kBlock) k_hash(const float* __restrict__ pos, 
     if (ids) ids[i] = i;
 }
 
-// sort_utils.cl:51-78 (cells were cleared before, sort_utils.cl:7-10)
+// sort_utils.cl:51-78 (cells were cleared before, sort_utils.cl:7-10). Also the cell code of each
+// particle and the list of bucket-run starts that the warp sweeps iterate.
 __global__ void __launch_bounds__(kBlock) k_reorder(const uint32_t* __restrict__ keys, const uint32_t* __restrict__ ids,
                                                     const float4* __restrict__ in_pos,
                                                     const float4* __restrict__ in_vel, uint32_t n,
                                                     float4* __restrict__ out_pos, float4* __restrict__ out_vel,
-                                                    uint2* __restrict__ cells, uint32_t bucket_count,
-                                                    Control* ctl) {
+                                                    uint2* __restrict__ cells, uint32_t* __restrict__ codes,
+                                                    uint32_t* __restrict__ groups, DevParams P, Control* ctl) {
     const uint32_t d = blockIdx.x * kBlock + threadIdx.x;
     if (d >= n) return;
     const uint32_t src = ids[d];
     const uint32_t key = keys[d];
-    if (src >= n || key >= bucket_count) {  // a sort that broke its contract: flag it, touch nothing
-        if (ctl) atomicOr(&ctl->status, 4u);
-        return;
+    const bool ok = src < n && key < P.bucket_count;
+    bool is_start = false;
+    if (ok) {
+        const float4 p = in_pos[src];
+        out_pos[d] = p;
+        if (in_vel) out_vel[d] = in_vel[src];
+        if (codes) {
+            const Cell c = cell_of(p.x, p.y, p.z, P);
+            codes[d] = cell_code(c.x, c.y, c.z);
+        }
+        is_start = d == 0 || key != keys[d - 1];
+        if (is_start) cells[key].x = d;
+        if (d == n - 1 || key != keys[d + 1]) cells[key].y = d + 1;
+    } else if (ctl) {  // a sort that broke its contract: flag it, touch nothing
+        atomicOr(&ctl->status, 4u);
     }
-    out_pos[d] = in_pos[src];
-    if (in_vel) out_vel[d] = in_vel[src];
-    if (d == 0 || key != keys[d - 1]) cells[key].x = d;
-    if (d == n - 1 || key != keys[d + 1]) cells[key].y = d + 1;
+    if (groups) {
+        const unsigned act = __activemask();
+        const unsigned m = __ballot_sync(act, is_start);
+        if (m) {
+            const int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
+            uint32_t base = 0;
+            if (lane == leader) base = atomicAdd(&ctl->n_groups, (unsigned)__popc(m));
+            base = __shfl_sync(act, base, leader);
+            if (is_start) groups[base + __popc(m & ((1u << lane) - 1u))] = d;
+        }
+    }
 }
 
 __global__ void k_begin(Control* ctl) {
@@ -70,6 +91,7 @@ __global__ void k_begin(Control* ctl) {
     ctl->blocks_done = 0;
     ctl->status = 0;
     ctl->guard_iters = 0;
+    ctl->n_groups = 0;
 }
 
 // pcisph.cl:65-92
@@ -412,10 +434,10 @@ void launch_hash(const float* pos, bool packed, uint32_t n, const DevParams& P, 
 }
 
 void launch_reorder(const uint32_t* keys, const uint32_t* ids, const float4* in_pos, const float4* in_vel,
-                    uint32_t n, float4* out_pos, float4* out_vel, uint2* cells, uint32_t bucket_count,
-                    Control* ctl, cudaStream_t s) {
+                    uint32_t n, float4* out_pos, float4* out_vel, uint2* cells, uint32_t* codes, uint32_t* groups,
+                    const DevParams& P, Control* ctl, cudaStream_t s) {
     if (!n) return;
-    k_reorder<<<grid_for(n), kBlock, 0, s>>>(keys, ids, in_pos, in_vel, n, out_pos, out_vel, cells, bucket_count,
+    k_reorder<<<grid_for(n), kBlock, 0, s>>>(keys, ids, in_pos, in_vel, n, out_pos, out_vel, cells, codes, groups, P,
                                              ctl);
 }
 

@@ -22,19 +22,23 @@ struct StepBuffers {
     float *rho, *press, *err;
     uint32_t *keys, *ids;            // sorted keys and source indices
     uint2* cells;                    // fluid cell table [bucket_count]
+    uint32_t* codes;                 // packed cell of each sorted particle (sweep.cuh cell_code)
+    uint32_t* groups;                // start of every bucket run (count in ctl->n_groups)
     // boundary
     float4 *b_pos, *bpf;
     float *b_press, *b_init;
     uint2* b_cells;                  // boundary cell table [bucket_count]
+    uint32_t* b_codes;
     Control* ctl;
 };
 
 // Kernels launched per call are reported through the return value (count), errors via cudaGetLastError.
 void launch_hash(const float* pos, bool packed, uint32_t n, const DevParams& P, uint32_t* keys, uint32_t* ids,
                  cudaStream_t s);
+// Also writes cell codes (if codes) and appends bucket-run starts to groups (if groups).
 void launch_reorder(const uint32_t* keys, const uint32_t* ids, const float4* in_pos, const float4* in_vel,
-                    uint32_t n, float4* out_pos, float4* out_vel, uint2* cells, uint32_t bucket_count,
-                    Control* ctl, cudaStream_t s);
+                    uint32_t n, float4* out_pos, float4* out_vel, uint2* cells, uint32_t* codes, uint32_t* groups,
+                    const DevParams& P, Control* ctl, cudaStream_t s);
 void launch_begin(Control* ctl, cudaStream_t s);
 void launch_density(const DevParams& P, const StepBuffers& b, cudaStream_t s);
 void launch_normal(const DevParams& P, const StepBuffers& b, cudaStream_t s);
@@ -47,6 +51,24 @@ void launch_pressure(const DevParams& P, const StepBuffers& b, cudaStream_t s);
 void launch_pressure_force(const DevParams& P, const StepBuffers& b, int mode, cudaGraphConditionalHandle cond,
                            bool use_cond, cudaStream_t s);
 void launch_pack(const DevParams& P, const StepBuffers& b, cudaStream_t s);
+// Warp-per-bucket sweeps (sweep_kernels.cu)
+struct SweepGrid {
+    int blocks[5];  // resident blocks (SMs x occupancy) of density, normal, force, pressure, pressure force
+    int warps[5];
+};
+cudaError_t sweep_configure(SweepGrid* g);
+struct SweepArgs;
+void launch_density_sweep(const DevParams& P, const StepBuffers& b, const SweepArgs& A, const SweepGrid& g,
+                          cudaStream_t s);
+void launch_normal_sweep(const DevParams& P, const StepBuffers& b, const SweepArgs& A, const SweepGrid& g,
+                         cudaStream_t s);
+void launch_force_sweep(const DevParams& P, const StepBuffers& b, const SweepArgs& A, const SweepGrid& g,
+                        cudaStream_t s);
+void launch_pressure_sweep(const DevParams& P, const StepBuffers& b, const SweepArgs& A, const SweepGrid& g,
+                           cudaStream_t s);
+void launch_pressure_force_sweep(const DevParams& P, const StepBuffers& b, const SweepArgs& A, const SweepGrid& g,
+                                 int mode, cudaGraphConditionalHandle cond, bool use_cond, cudaStream_t s);
+
 void launch_pack3_to4(const float* in3, float4* out, uint32_t n, cudaStream_t s);
 void launch_unpack4_to3(const float4* in, float* out3, uint32_t n, cudaStream_t s);
 

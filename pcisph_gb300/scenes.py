@@ -111,8 +111,14 @@ def config0():
 
 
 def config1():
-    """1,048,576 particles, d = 0.005 m, dt = 2.5e-4 s, 500 steps (same physical box)."""
-    return dam_break(128, seed=0, delta_t=2.5e-4, steps=500)
+    """1,048,576 particles, d = 0.005 m, dt = 2.5e-4 s, 500 steps, in the config-0 box.
+
+    A 128^3 lattice at d = 0.005 m would hold 2,097,152 particles; the workload keeps the stated
+    particle count (2^20) and spacing and halves the depth: 128 x 128 x 64 (0.64 x 0.64 x 0.32 m).
+    """
+    d = 0.005
+    pos = lattice_block(128, 128, 64, d, (0.0, 0.0, 0.0), seed=0)
+    return Scene("dam_break_128x128x64", pos, d, 2.5e-4, (0.0, 0.0, 0.0), (1.6, 1.2, 0.8), steps=500)
 
 
 def config2():

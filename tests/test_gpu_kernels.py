@@ -105,9 +105,10 @@ def _load_case(golden, case, **kw):
     return g, p, f
 
 
+@pytest.mark.parametrize("variant", [0, 1])
 @pytest.mark.parametrize("case", ["step_boundary", "step_fluid"])
-def test_kernel_chain_vs_reference(golden, case):
-    g, p, f = _load_case(golden, case)
+def test_kernel_chain_vs_reference(golden, case, variant):
+    g, p, f = _load_case(golden, case, kernel_variant=variant)
     B = p.boundary_count
     eq = np.testing.assert_array_equal
     f.run_stage("sort")
@@ -162,7 +163,7 @@ def test_kernel_chain_vs_reference(golden, case):
         else:
             errs["x_new"] = assert_close("x_new", f.get_field("position"), g["x_new"])
             errs["v_new"] = assert_close("v_new", f.get_field("velocity"), g["v_new"])
-    print(case, {k: f"{v:.1e}" for k, v in errs.items()})
+    print(case, variant, {k: f"{v:.1e}" for k, v in errs.items()})
 
 
 def test_boundary_self_density_computed(golden):
@@ -181,10 +182,10 @@ def test_boundary_self_density_computed(golden):
 
 
 @pytest.mark.parametrize("case", ["step_boundary", "step_fluid"])
-@pytest.mark.parametrize("loop_mode", [0, 1])
-def test_full_steps_vs_reference(golden, case, loop_mode):
+@pytest.mark.parametrize("loop_mode,variant", [(0, 0), (1, 0), (0, 1)])
+def test_full_steps_vs_reference(golden, case, loop_mode, variant):
     """Fluid::update sequence (min 3 / max 7 iterations, no walls) against the reference's full steps."""
-    g, p, f = _load_case(golden, case, loop_mode=loop_mode)
+    g, p, f = _load_case(golden, case, loop_mode=loop_mode, kernel_variant=variant)
     k = 0
     while f"step{k}_iters" in g:
         f.update()
@@ -220,7 +221,8 @@ def test_graph_and_host_loop_identical():
 # ------------------------------------------------------------------------------------------- full step vs FP64
 
 
-def test_full_step_error_vs_fp64(oracle):
+@pytest.mark.parametrize("variant", [0, 1])
+def test_full_step_error_vs_fp64(oracle, variant):
     """One step (fixed 4 iterations, walls on) from identical state: the GPU's error against the FP64 rerun
     is of the order of the FP32 oracle's own error against it."""
     sc = scenes.small_dam(12, seed=4)
@@ -233,7 +235,7 @@ def test_full_step_error_vs_fp64(oracle):
     s64 = oracle.new_state(p, sc.fluid_pos, vel, dtype=np.float64)
     oracle.step(p, opts, s32)
     oracle.step(p, opts, s64)
-    f = fluid_like(p, min_iters=4, max_iters=4, walls=True, box_hi=sc.box_hi)
+    f = fluid_like(p, min_iters=4, max_iters=4, walls=True, box_hi=sc.box_hi, kernel_variant=variant)
     f.set_fluid_state(sc.fluid_pos, vel)
     f.update()
     assert f.stats().iterations == 4
@@ -249,36 +251,49 @@ def test_full_step_error_vs_fp64(oracle):
     print({k: f"gpu {a:.1e} / fp32 oracle {b:.1e}" for k, (a, b) in report.items()})
 
 
-def test_long_run_statistics_vs_oracle(oracle):
-    """200 steps of a small dam break: trajectories diverge (chaos), statistics must not."""
+@pytest.mark.parametrize("variant", [0, 1])
+def test_long_run_statistics_vs_oracle(oracle, variant):
+    """200 steps of a small dam break. SPH trajectories are chaotic: the oracle itself, with one coordinate moved
+    by 1 ulp, drifts from its unperturbed run (that drift is measured here). The GPU must stay within 3x that
+    drift in kinetic energy and centre of mass, hold every step at <= 1% density error, and need the same mean
+    number of corrective iterations (within 0.5)."""
     sc = scenes.small_dam(12, seed=5)
     p = oracle.derive_params(sc.particle_radius, sc.rest_density, sc.fluid_count, 0, sc.delta_t, sc.gravity,
                              sc.viscosity_constant(), sc.surface_tension)
     opts = make_options(threshold=0.01, min_iters=3, max_iters=50, walls=True, box_hi=sc.box_hi)
-    s = oracle.new_state(p, sc.fluid_pos, np.zeros((sc.fluid_count, 3)))
-    f = fluid_like(p, min_iters=3, max_iters=50, walls=True, box_hi=sc.box_hi)
+    zero = np.zeros((sc.fluid_count, 3))
+    s = oracle.new_state(p, sc.fluid_pos, zero)
+    bumped = sc.fluid_pos.copy()
+    bumped[100, 0] = np.nextafter(bumped[100, 0], np.float32(1))
+    sb = oracle.new_state(p, bumped, zero)
+    f = fluid_like(p, min_iters=3, max_iters=50, walls=True, box_hi=sc.box_hi, kernel_variant=variant)
     f.set_fluid_state(sc.fluid_pos, None)
-    ke_o, ke_g, com_o, com_g, it_o, it_g = [], [], [], [], [], []
+    ke = {"o": [], "b": [], "g": []}
+    com = {"o": [], "b": [], "g": []}
+    it_o, it_g = [], []
     for k in range(200):
         st_o = oracle.step(p, opts, s)
+        oracle.step(p, opts, sb)
         f.update()
         st_g = f.stats()
-        assert st_o.max_err / p.rest_density < 0.01 and st_g.max_density_error < 0.01
+        assert st_o.max_err / p.rest_density < 0.01 and st_g.max_density_error < 0.01 and st_g.status == 0
         it_o.append(st_o.iterations)
         it_g.append(st_g.iterations)
         if k % 10 == 9:
-            ke_o.append(kinetic_energy(p.particle_mass, s["f_vel"]))
-            ke_g.append(kinetic_energy(p.particle_mass, f.get_field("velocity")))
-            com_o.append(s["f_pos"].astype(np.float64).mean(0))
-            com_g.append(f.get_field("position").astype(np.float64).mean(0))
-    ke_o, ke_g = np.array(ke_o), np.array(ke_g)
-    com_o, com_g = np.array(com_o), np.array(com_g)
-    ke_rel = np.abs(ke_g - ke_o).max() / ke_o.max()
-    com_abs = np.abs(com_g - com_o).max()
-    print(f"KE rel diff {ke_rel:.2e}, COM abs diff {com_abs:.2e} m, mean iters gpu {np.mean(it_g):.3f} "
-          f"oracle {np.mean(it_o):.3f}")
-    assert ke_rel < 0.02
-    assert com_abs < 2e-3
+            for key, vel, pos in (("o", s["f_vel"], s["f_pos"]), ("b", sb["f_vel"], sb["f_pos"]),
+                                  ("g", f.get_field("velocity"), f.get_field("position"))):
+                ke[key].append(kinetic_energy(p.particle_mass, vel))
+                com[key].append(np.asarray(pos, np.float64).mean(0))
+    ke = {k: np.array(v) for k, v in ke.items()}
+    com = {k: np.array(v) for k, v in com.items()}
+    chaos_ke = np.abs(ke["b"] - ke["o"]).max() / ke["o"].max()
+    chaos_com = np.abs(com["b"] - com["o"]).max()
+    gpu_ke = np.abs(ke["g"] - ke["o"]).max() / ke["o"].max()
+    gpu_com = np.abs(com["g"] - com["o"]).max()
+    print(f"KE drift: 1-ulp oracle {chaos_ke:.2e}, gpu {gpu_ke:.2e}; COM drift: 1-ulp oracle {chaos_com:.2e} m, "
+          f"gpu {gpu_com:.2e} m; mean iterations gpu {np.mean(it_g):.3f} oracle {np.mean(it_o):.3f}")
+    assert gpu_ke <= 3 * chaos_ke + 1e-3
+    assert gpu_com <= 3 * chaos_com + 1e-5
     assert abs(np.mean(it_g) - np.mean(it_o)) < 0.5
 
 
