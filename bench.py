@@ -53,6 +53,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=20.0, help="bound of the CPU baseline sample")
+    ap.add_argument("--variant", type=int, default=0, help="neighbour-sweep kernel variant (pcisph_options)")
     return ap.parse_args()
 
 
@@ -198,7 +199,7 @@ def main():
     stream = torch.cuda.Stream()  # a real stream: the library launches on it, the events are recorded on it
     torch.cuda.set_stream(stream)
     f = Fluid(local, stream=stream.cuda_stream)
-    setup_scene(f, sc)
+    setup_scene(f, sc, kernel_variant=args.variant)
     sampler = ClockSampler(local)
     sampler.start()
     for _ in range(args.warmup):
@@ -293,6 +294,7 @@ def main():
             "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded jittered lattice)",
             "config": {"workload": WORKLOAD, "particles": N, "parallelism": f"replicas x{world}",
+                       "kernel_variant": args.variant,
                        "mean_iterations": iters, "max_density_error_last": st1.max_density_error,
                        "step_ms_min_median_max": [min(step_ms), statistics.median(step_ms), max(step_ms)],
                        "converged_all_steps": (status_bits & 1) == 0, "status_bits": status_bits,
