@@ -237,6 +237,18 @@ PCISPH_API int pcisph_radixsort_enqueue(pcisph_radixsort* sorter, uint32_t* keys
 /* Digit width in bits (4..11); 0 selects the tuned default. */
 PCISPH_API int pcisph_radixsort_set_digit_bits(pcisph_radixsort* sorter, int bits);
 
+/* The same stable sort for callers that must not allocate device memory when they sort (a pool allocator
+ * owns the device's memory, or an allocation would stall a latency-critical loop). No counterpart in the
+ * reference. Its scratch is a fixed device array inside this library, reserved on every device that loads
+ * the library until the process exits; sorts of more than PCISPH_NOALLOC_SORT_MAX_ELEMENTS keys are
+ * rejected with PCISPH_ERR_INVALID_ARG. The first call on a device looks up that array's address (make it
+ * before any stream capture). All calls share the array: calls that overlap on the GPU race, so order
+ * them on one stream. Keys, values, max_bits and stream as in pcisph_radixsort_enqueue, on the current
+ * device. */
+#define PCISPH_NOALLOC_SORT_MAX_ELEMENTS (1u << 20)
+PCISPH_API int pcisph_radixsort_enqueue_noalloc(uint32_t* keys, uint32_t* values, size_t elements,
+                                                unsigned int max_bits, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

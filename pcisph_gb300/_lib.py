@@ -129,6 +129,7 @@ def load():
         "pcisph_radixsort_destroy": ([vp], None),
         "pcisph_radixsort_enqueue": ([vp, vp, vp, sz, C.c_uint, vp], i32),
         "pcisph_radixsort_set_digit_bits": ([vp, i32], i32),
+        "pcisph_radixsort_enqueue_noalloc": ([vp, vp, sz, C.c_uint, vp], i32),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)

@@ -754,6 +754,10 @@ struct pcisph_ctx {
     }
 };
 
+namespace pcisph {
+int report_error(int code, const std::string& msg) { return fail(code, msg); }
+}  // namespace pcisph
+
 // ====================================================================== C ABI
 extern "C" {
 

@@ -1,0 +1,55 @@
+"""The allocation-free radix sort entry point against the allocating one, through the C ABI.
+
+pcisph_radixsort_enqueue_noalloc exists for callers that must not allocate device memory while they sort
+(a pool allocator owns the device's memory, or an allocation would stall a latency-critical loop); its
+scratch is a fixed array inside the library. This file is collected last so that a run stopping at the
+first failure has run every other test; it also passes alone in a fresh process.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from pcisph_gb300 import RadixSort, _lib
+
+pytestmark = pytest.mark.gpu
+MAX = 1 << 20  # PCISPH_NOALLOC_SORT_MAX_ELEMENTS
+
+
+def _dev(a):
+    torch = pytest.importorskip("torch")
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def _noalloc(keys, vals, n, max_bits):
+    L = _lib.load()
+    return L.pcisph_radixsort_enqueue_noalloc(C.c_void_p(keys.data_ptr()), C.c_void_p(vals.data_ptr()), n,
+                                              max_bits, None)
+
+
+def test_noalloc_sort_matches_allocating_sort_twice():
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(2024)
+    ref_sorter = RadixSort(0)
+    # two calls in a row with different inputs: the second must not see anything left by the first
+    for n, hi, bits in [(MAX, 1 << 19, 19), (300001, 1 << 32, 0)]:
+        keys = rng.integers(0, hi, n, dtype=np.uint64).astype(np.uint32)
+        vals = rng.integers(0, 1 << 32, n, dtype=np.uint64).astype(np.uint32)
+        k1, v1 = _dev(keys.view(np.int32)), _dev(vals.view(np.int32))
+        k2, v2 = k1.clone(), v1.clone()
+        assert _noalloc(k1, v1, n, bits) == _lib.OK, _lib.load().pcisph_last_error()
+        ref_sorter.enqueue(k2, v2, n, max_bits=bits)
+        torch.cuda.synchronize()
+        # integer results: exact agreement (tolerance zero)
+        np.testing.assert_array_equal(k1.cpu().numpy(), k2.cpu().numpy())
+        np.testing.assert_array_equal(v1.cpu().numpy(), v2.cpu().numpy())
+        order = np.argsort(keys, kind="stable")
+        np.testing.assert_array_equal(k1.cpu().numpy().view(np.uint32), keys[order])
+
+
+def test_noalloc_sort_rejects_more_than_its_maximum():
+    torch = pytest.importorskip("torch")
+    k = torch.zeros(MAX + 1, dtype=torch.int32, device="cuda")
+    v = torch.zeros(MAX + 1, dtype=torch.int32, device="cuda")
+    assert _noalloc(k, v, MAX + 1, 0) == _lib.ERR_INVALID_ARG
+    assert b"exceed its fixed scratch" in _lib.load().pcisph_last_error()
