@@ -53,7 +53,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=20.0, help="bound of the CPU baseline sample")
-    ap.add_argument("--variant", type=int, default=0, help="neighbour-sweep kernel variant (pcisph_options)")
+    ap.add_argument("--variant", type=int, default=2, help="neighbour-sweep kernel variant (pcisph_options)")
     return ap.parse_args()
 
 

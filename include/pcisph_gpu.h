@@ -88,8 +88,11 @@ typedef struct pcisph_options {
     int32_t loop_mode;             /* default 0: the corrective loop is decided on the device (CUDA graph with
                                       a conditional while node); 1: host reads the decision each iteration,
                                       like the reference (Fluid.cpp:300-306) */
-    int32_t kernel_variant;        /* default 0: neighbour sweeps with one warp per bucket run and shared-memory
-                                      staging; 1: one thread per particle walking the 27 buckets */
+    int32_t kernel_variant;        /* neighbour sweeps. default 2: per-particle neighbour lists built by the
+                                      density sweep (27-bucket walk), reused by the later sweeps of the step;
+                                      0: one warp per bucket run with shared-memory staging; 1: one thread per
+                                      particle walking the 27 buckets in every sweep */
+    float list_skin;               /* variant 2: list radius = kernel_radius * (1 + list_skin), default 0.25 */
 } pcisph_options;
 
 typedef struct pcisph_step_stats {
@@ -99,6 +102,9 @@ typedef struct pcisph_step_stats {
     uint32_t status_all;         /* OR of the status bits of every step since the last reset */
     uint64_t steps;              /* steps done by this context */
     uint64_t total_iterations;   /* corrective iterations summed over those steps */
+    uint64_t list_fallbacks;     /* variant 2: pressure sweeps in which some predicted displacement exceeded
+                                    half the list skin (the particles near it walked the buckets) */
+    uint64_t fast_particles;     /* variant 2: predictions that moved more than half the list skin */
 } pcisph_step_stats;
 
 /* ----------------------------------------------------------- enums */

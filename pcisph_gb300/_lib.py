@@ -49,12 +49,14 @@ class SimParams(C.Structure):
 class Options(C.Structure):
     _fields_ = [("min_iterations", C.c_int32), ("max_iterations", C.c_int32), ("walls", C.c_int32),
                 ("box_lo", C.c_float * 3), ("box_hi", C.c_float * 3), ("restitution", C.c_float),
-                ("boundary_self_density", C.c_int32), ("loop_mode", C.c_int32), ("kernel_variant", C.c_int32)]
+                ("boundary_self_density", C.c_int32), ("loop_mode", C.c_int32), ("kernel_variant", C.c_int32),
+                ("list_skin", C.c_float)]
 
 
 class StepStats(C.Structure):
     _fields_ = [("iterations", C.c_int32), ("max_density_error", C.c_float), ("status", C.c_uint32),
-                ("status_all", C.c_uint32), ("steps", C.c_uint64), ("total_iterations", C.c_uint64)]
+                ("status_all", C.c_uint32), ("steps", C.c_uint64), ("total_iterations", C.c_uint64),
+                ("list_fallbacks", C.c_uint64), ("fast_particles", C.c_uint64)]
 
 
 class KernelTime(C.Structure):

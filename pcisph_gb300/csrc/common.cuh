@@ -23,6 +23,9 @@ struct DevParams {
     uint32_t fluid_count, boundary_count, bucket_count;
     // modulo by bucket_count
     uint32_t bk_magic, bk_shift;
+    // neighbour lists (kernel_variant 2): capacity per particle, radius h (1 + skin) and its square
+    uint32_t list_cap;
+    float list_r, list_r2, list_half_skin;
     // options
     int min_iters, max_iters, walls;
     float box_lo[3], box_hi[3], restitution, threshold;
@@ -41,6 +44,9 @@ struct Control {
     unsigned long long total_iters;
     unsigned int guard_iters;    // loop iterations counted by the pressure-force kernel (bounds the graph loop)
     unsigned int n_groups;       // bucket runs listed by the reorder kernel this step
+    unsigned int max_disp_bits;  // float bits of max |x* - x| this step (neighbour-list validity)
+    unsigned long long list_fallbacks;  // pressure sweeps in which some particle moved more than skin / 2
+    unsigned long long fast_particles;  // predictions that moved more than skin / 2 (each flags its bucket)
 };
 
 __host__ __device__ inline void magic_for(uint32_t d, uint32_t* magic, uint32_t* shift) {

@@ -47,6 +47,7 @@ int fail(int code, const std::string& msg) {
 size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 
 const float kPi = 3.14159265358979323846f;  // utils/constants.h:4
+constexpr uint32_t kListCap = 96;           // neighbour-list entries per particle (multiple of 4)
 
 // Fluid.cpp:125-133
 uint32_t sort_bit_count_ref(uint32_t elements) {
@@ -175,7 +176,7 @@ struct pcisph_ctx {
     uint32_t fluid_loaded = 0xFFFFFFFFu, boundary_loaded = 0xFFFFFFFFu;
     uint32_t fluid_cap_n = 0, fluid_cap_bk = 0, boundary_cap_n = 0, boundary_cap_bk = 0;
 
-    DeviceBlock fluid_block, boundary_block, misc_block, sort_block, staging_block;
+    DeviceBlock fluid_block, boundary_block, misc_block, sort_block, staging_block, list_block;
     StepBuffers b{};
     float4* b_pos_in = nullptr;
     uint32_t *f_keys = nullptr, *f_ids = nullptr, *b_keys = nullptr, *b_ids = nullptr;
@@ -185,11 +186,54 @@ struct pcisph_ctx {
     RadixSorter sorter;
     DevParams P{};
     SweepGrid sweep_grid{};
+    uint32_t* morton = nullptr;   // Morton codes for the working order (list block)
+    uint32_t* work_buf = nullptr;
+    RadixSorter work_sorter;      // sorts the Morton codes (allocates its scratch on first use)
+    size_t list_n = 0;
+    static constexpr uint64_t kWorkOrderInterval = 16;
 
     SweepArgs sweep_args() const {
         return SweepArgs{b.groups, &b.ctl->n_groups, sorted_keys, b.cells, b.b_cells, b.codes, b.b_codes};
     }
     bool warp_sweeps() const { return opts.kernel_variant == 0; }
+    bool list_sweeps() const { return opts.kernel_variant == 2; }
+
+    int ensure_lists() {
+        if (!list_sweeps()) return PCISPH_OK;
+        const size_t n = params.fluid_count;
+        const size_t bytes = align256(n * P.list_cap * 4) + 3 * align256(n * 4) + align256(params.bucket_count);
+        if (list_block.p && list_block.cap >= bytes && list_n == n) return PCISPH_OK;
+        CUDA_TRY(cudaStreamSynchronize(stream()));
+        if (list_block.ensure(bytes) != cudaSuccess)
+            return fail(PCISPH_ERR_OOM, "device allocation of the neighbour lists failed");
+        Carver c{static_cast<unsigned char*>(list_block.p)};
+        b.nbr = c.take<uint32_t>(n * P.list_cap);
+        b.nbr_count = c.take<uint32_t>(n);
+        work_buf = c.take<uint32_t>(n);
+        morton = c.take<uint32_t>(n);
+        b.bucket_fast = c.take<unsigned char>(params.bucket_count);
+        b.work = nullptr;  // identity working order
+        CUDA_TRY(cudaGetLastError());
+        list_n = n;
+        graph_valid = false;
+        return PCISPH_OK;
+    }
+
+    // Working order of the list sweeps: this step's sorted particles ordered by the Morton code of their
+    // cell. Run after a step (stream-ordered), used by the next steps; refreshed every kWorkOrderInterval.
+    int refresh_work_order(cudaStream_t s) {
+        if (!list_sweeps() || !work_buf) return PCISPH_OK;
+        b.work = work_buf;
+        const uint32_t n = params.fluid_count;
+        launch_morton(b.pos, n, P, morton, s);
+        uint32_t *sk = nullptr, *sv = nullptr;
+        // a sorter of its own: the step's sorter scratch holds this step's sorted keys and ids
+        cudaError_t e = work_sorter.sort(morton, b.work, n, 30, true, s, &sk, &sv);
+        if (e != cudaSuccess) return fail(PCISPH_ERR_CUDA, std::string("work-order sort: ") + cudaGetErrorString(e));
+        if (sv != b.work) CUDA_TRY(cudaMemcpyAsync(b.work, sv, (size_t)n * 4, cudaMemcpyDeviceToDevice, s));
+        host_launches += 1 + work_sorter.last_launches();
+        return PCISPH_OK;
+    }
 
     cudaGraphExec_t graph_exec = nullptr;
     bool graph_valid = false;
@@ -313,6 +357,11 @@ struct pcisph_ctx {
         }
         d.restitution = opts.restitution;
         d.threshold = threshold;
+        d.list_cap = kListCap;
+        d.list_r = params.kernel_radius * (1.f + opts.list_skin);
+        d.list_r2 = d.list_r * d.list_r;
+        // half the skin, less a margin for the rounding of |x_i - x_j| and |x* - x| (relative 1e-6 of h)
+        d.list_half_skin = 0.5f * params.kernel_radius * opts.list_skin - 1e-6f * params.kernel_radius;
         graph_valid = false;
     }
 
@@ -413,6 +462,7 @@ struct pcisph_ctx {
         launch_begin(b.ctl, s);
         ++nl;
         if (cudaMemsetAsync(b.cells, 0, (size_t)params.bucket_count * 8, s) != cudaSuccess) return -1;
+        if (list_sweeps() && cudaMemsetAsync(b.bucket_fast, 0, params.bucket_count, s) != cudaSuccess) return -1;
         uint32_t *sk = nullptr, *sv = nullptr;
         int r = sort_set(b.state_pos, N, f_keys, f_ids, &sk, &sv, s);
         if (r < 0) return -1;
@@ -421,7 +471,10 @@ struct pcisph_ctx {
         sorted_ids = sv;
         timed("reorder", s, [&] { launch_reorder(sk, sv, b.state_pos, b.state_vel, N, b.pos, b.vel, b.cells, b.codes, b.groups, P, b.ctl, s); });
         const SweepArgs A = sweep_args();
-        if (warp_sweeps()) {
+        if (list_sweeps()) {
+            timed("density", s, [&] { launch_density_list(P, b, s); });
+            timed("normal", s, [&] { launch_normal_list(P, b, s); });
+        } else if (warp_sweeps()) {
             timed("density", s, [&] { launch_density_sweep(P, b, A, sweep_grid, s); });
             timed("normal", s, [&] { launch_normal_sweep(P, b, A, sweep_grid, s); });
         } else {
@@ -429,7 +482,8 @@ struct pcisph_ctx {
             timed("normal", s, [&] { launch_normal(P, b, s); });
         }
         if (B && cudaMemsetAsync(b.b_press, 0, (size_t)B * 4, s) != cudaSuccess) return -1;
-        if (warp_sweeps()) timed("force", s, [&] { launch_force_sweep(P, b, A, sweep_grid, s); });
+        if (list_sweeps()) timed("force", s, [&] { launch_force_list(P, b, s); });
+        else if (warp_sweeps()) timed("force", s, [&] { launch_force_sweep(P, b, A, sweep_grid, s); });
         else timed("force", s, [&] { launch_force(P, b, s); });
         nl += 4;
         if (cudaGetLastError() != cudaSuccess) return -1;
@@ -442,7 +496,10 @@ struct pcisph_ctx {
             timed("boundary_pressure", s, [&] { launch_boundary_pressure(P, b, s); });
             ++nl;
         }
-        if (warp_sweeps()) {
+        if (list_sweeps()) {
+            timed("pressure", s, [&] { launch_pressure_list(P, b, s); });
+            timed("pressure_force", s, [&] { launch_pressure_force_list(P, b, 0, cond, use_cond, s); });
+        } else if (warp_sweeps()) {
             const SweepArgs A = sweep_args();
             timed("pressure", s, [&] { launch_pressure_sweep(P, b, A, sweep_grid, s); });
             timed("pressure_force", s, [&] { launch_pressure_force_sweep(P, b, A, sweep_grid, 0, cond, use_cond, s); });
@@ -524,6 +581,8 @@ struct pcisph_ctx {
         int rc = check_consistent();
         if (rc) return rc;
         if (params.fluid_count == 0) return PCISPH_OK;  // Fluid.cpp:117-118
+        rc = ensure_lists();
+        if (rc) return rc;
         cudaStream_t s = stream();
         if (boundary_updated && params.boundary_count > 0) {
             rc = boundary_sort(s);
@@ -566,6 +625,8 @@ struct pcisph_ctx {
         }
         int rc = check_consistent();
         if (rc) return rc;
+        rc = ensure_lists();
+        if (rc) return rc;
         cudaStream_t s = stream();
         const uint32_t N = params.fluid_count;
         switch (stage) {
@@ -576,6 +637,7 @@ struct pcisph_ctx {
                 }
                 launch_begin(b.ctl, s);
                 CUDA_TRY(cudaMemsetAsync(b.cells, 0, (size_t)params.bucket_count * 8, s));
+                if (list_sweeps()) CUDA_TRY(cudaMemsetAsync(b.bucket_fast, 0, params.bucket_count, s));
                 uint32_t *sk = nullptr, *sv = nullptr;
                 int nl = sort_set(b.state_pos, N, f_keys, f_ids, &sk, &sv, s);
                 if (nl < 0) return PCISPH_ERR_CUDA;
@@ -586,28 +648,33 @@ struct pcisph_ctx {
                 break;
             }
             case PCISPH_STAGE_DENSITY:
-                if (warp_sweeps()) launch_density_sweep(P, b, sweep_args(), sweep_grid, s);
+                if (list_sweeps()) launch_density_list(P, b, s);
+                else if (warp_sweeps()) launch_density_sweep(P, b, sweep_args(), sweep_grid, s);
                 else launch_density(P, b, s);
                 ++host_launches;
                 break;
             case PCISPH_STAGE_NORMAL:
-                if (warp_sweeps()) launch_normal_sweep(P, b, sweep_args(), sweep_grid, s);
+                if (list_sweeps()) launch_normal_list(P, b, s);
+                else if (warp_sweeps()) launch_normal_sweep(P, b, sweep_args(), sweep_grid, s);
                 else launch_normal(P, b, s);
                 ++host_launches;
                 break;
             case PCISPH_STAGE_FORCE:
-                if (warp_sweeps()) launch_force_sweep(P, b, sweep_args(), sweep_grid, s);
+                if (list_sweeps()) launch_force_list(P, b, s);
+                else if (warp_sweeps()) launch_force_sweep(P, b, sweep_args(), sweep_grid, s);
                 else launch_force(P, b, s);
                 ++host_launches;
                 break;
             case PCISPH_STAGE_BOUNDARY_PRESSURE: launch_boundary_pressure(P, b, s); ++host_launches; break;
             case PCISPH_STAGE_PRESSURE:
-                if (warp_sweeps()) launch_pressure_sweep(P, b, sweep_args(), sweep_grid, s);
+                if (list_sweeps()) launch_pressure_list(P, b, s);
+                else if (warp_sweeps()) launch_pressure_sweep(P, b, sweep_args(), sweep_grid, s);
                 else launch_pressure(P, b, s);
                 ++host_launches;
                 break;
             case PCISPH_STAGE_PRESSURE_FORCE:
-                if (warp_sweeps()) launch_pressure_force_sweep(P, b, sweep_args(), sweep_grid, arg ? 2 : 1, 0, false, s);
+                if (list_sweeps()) launch_pressure_force_list(P, b, arg ? 2 : 1, 0, false, s);
+                else if (warp_sweeps()) launch_pressure_force_sweep(P, b, sweep_args(), sweep_grid, arg ? 2 : 1, 0, false, s);
                 else launch_pressure_force(P, b, arg ? 2 : 1, 0, false, s);
                 ++host_launches;
                 break;
@@ -731,6 +798,8 @@ struct pcisph_ctx {
         out->status_all = host_ctl->status_all;
         out->steps = host_ctl->steps;
         out->total_iterations = host_ctl->total_iters;
+        out->list_fallbacks = host_ctl->list_fallbacks;
+        out->fast_particles = host_ctl->fast_particles;
         return PCISPH_OK;
     }
 
@@ -748,6 +817,7 @@ struct pcisph_ctx {
         misc_block.release();
         sort_block.release();
         staging_block.release();
+        list_block.release();
         if (host_ctl) cudaFreeHost(host_ctl);
         if (capture_stream) cudaStreamDestroy(capture_stream);
         if (own_stream) cudaStreamDestroy(own_stream);
@@ -793,6 +863,8 @@ int pcisph_default_options(pcisph_options* o) {
     o->restitution = 0.5f;
     o->boundary_self_density = 0;
     o->loop_mode = 0;
+    o->kernel_variant = 2;
+    o->list_skin = 0.25f;
     return PCISPH_OK;
 }
 
@@ -867,8 +939,10 @@ int pcisph_set_options(pcisph_ctx* ctx, const pcisph_options* o) {
     if (o->max_iterations < 1 || o->min_iterations < 1 || o->max_iterations > 10000)
         return fail(PCISPH_ERR_INVALID_ARG, "iteration limits must be in 1..10000");
     if (o->loop_mode != 0 && o->loop_mode != 1) return fail(PCISPH_ERR_INVALID_ARG, "loop_mode must be 0 or 1");
-    if (o->kernel_variant != 0 && o->kernel_variant != 1)
-        return fail(PCISPH_ERR_INVALID_ARG, "kernel_variant must be 0 or 1");
+    if (o->kernel_variant < 0 || o->kernel_variant > 2)
+        return fail(PCISPH_ERR_INVALID_ARG, "kernel_variant must be 0, 1 or 2");
+    if (!(o->list_skin >= 0.f && o->list_skin <= 2.f))
+        return fail(PCISPH_ERR_INVALID_ARG, "list_skin must be in [0, 2]");
     const bool bsd_changed = o->boundary_self_density != ctx->opts.boundary_self_density;
     ctx->opts = *o;
     if (bsd_changed) ctx->boundary_updated = true;

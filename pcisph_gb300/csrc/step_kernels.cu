@@ -15,6 +15,7 @@
 //   pressure force then predicts for the next iteration, or integrates (with
 //                  optional walls) when the loop has stopped
 #include "step_kernels.cuh"
+#include "pair_terms.cuh"
 #include "sweep.cuh"
 
 namespace pcisph {
@@ -92,6 +93,7 @@ __global__ void k_begin(Control* ctl) {
     ctl->status = 0;
     ctl->guard_iters = 0;
     ctl->n_groups = 0;
+    ctl->max_disp_bits = 0;
 }
 
 // pcisph.cl:65-92
@@ -130,21 +132,10 @@ __global__ void __launch_bounds__(kBlock) k_normal(DevParams P, const uint2* __r
     const float4 xi = pr4[i];
     const Cell c = cell_of(xi.x, xi.y, xi.z, P);
     const float h2 = P.h2;
-    float nx = 0.f, ny = 0.f, nz = 0.f;
-    for_each_neighbour(cells, c, P, [&](uint32_t j) {
-        const float4 o = __ldg(&pr4[j]);
-        const float dx = xi.x - o.x, dy = xi.y - o.y, dz = xi.z - o.z;
-        const float r2 = dx * dx + dy * dy + dz * dz;
-        if (r2 <= h2) {
-            const float s = (r2 - h2) * (r2 - h2);
-            const float inv = __frcp_rn(o.w);
-            nx += (s * dx) * inv;
-            ny += (s * dy) * inv;
-            nz += (s * dz) * inv;
-        }
-    });
+    float3 n = make_float3(0.f, 0.f, 0.f);
+    for_each_neighbour(cells, c, P, [&](uint32_t j) { normal_term(xi.x, xi.y, xi.z, __ldg(&pr4[j]), h2, n); });
     const float scale = P.h * P.particle_mass * P.poly6_d1_norm;
-    normal[i] = make_float4(nx * scale, ny * scale, nz * scale, 0.f);
+    normal[i] = make_float4(n.x * scale, n.y * scale, n.z * scale, 0.f);
 }
 
 // pcisph.cl:121-173, then pcisph.cl:175-193 with F_p = 0 (the first predict)
@@ -158,31 +149,14 @@ __global__ void __launch_bounds__(kBlock) k_force(DevParams P, const uint2* __re
     const float3 vi = f3(vel[i]);
     const float3 ni = f3(normal[i]);
     const Cell c = cell_of(xi.x, xi.y, xi.z, P);
-    const float h = P.h, h2 = P.h2, rho0 = P.rest_density, ri = xi.w;
-    float3 visc = make_float3(0.f, 0.f, 0.f), coh = visc, curv = visc;
+    ForceAccum fa{make_float3(0.f, 0.f, 0.f), make_float3(0.f, 0.f, 0.f), make_float3(0.f, 0.f, 0.f)};
     for_each_neighbour(cells, c, P, [&](uint32_t j) {
-        const float4 o = __ldg(&pr4[j]);
-        const float3 d = make_float3(xi.x - o.x, xi.y - o.y, xi.z - o.z);
-        const float r2 = dot3(d, d);
-        if (r2 <= h2) {
-            const float dist = sqrtf(r2);
-            const float rj = o.w;
-            const float3 vj = f3(__ldg(&vel[j]));
-            if (rj > 0.0001f) visc = visc + (vj - vi) * ((h - dist) / rj);
-            if (dist > 0.0001f && dist < h) {
-                const float3 nj = f3(__ldg(&normal[j]));
-                const float corr = 2.f * rho0 / (ri + rj);
-                const float stk = surface_tension_kernel(dist, h, P.st_term);
-                const float3 dir = d / dist;
-                coh = coh + (corr * stk) * dir;
-                curv = curv + corr * (ni - nj);
-            }
-        }
+        force_term(xi, vi, ni, __ldg(&pr4[j]), f3(__ldg(&vel[j])), f3(__ldg(&normal[j])), P, fa);
     });
     const float m = P.particle_mass;
-    visc = visc * (P.viscosity * m * P.visc_d2_norm);
-    coh = coh * (-P.st_coeff * m * m * P.st_norm);
-    curv = curv * (-P.st_coeff * m);
+    const float3 visc = fa.visc * (P.viscosity * m * P.visc_d2_norm);
+    const float3 coh = fa.coh * (-P.st_coeff * m * m * P.st_norm);
+    const float3 curv = fa.curv * (-P.st_coeff * m);
     const float3 fo = make_float3(0.f, m * P.gravity, 0.f) + visc + (coh + curv);
     f_other[i] = f4(fo, 0.f);
     press[i] = 0.f;
@@ -337,27 +311,13 @@ __global__ void __launch_bounds__(kBlock) k_pressure_force(DevParams P, const ui
     if (i >= P.fluid_count) return;
     const float4 xi = pf4[i];
     const Cell c = cell_of(xi.x, xi.y, xi.z, P);
-    const float h = P.h, h2 = P.h2, fi = xi.w;
-    float fx = 0.f, fy = 0.f, fz = 0.f;
-    auto body = [&](const float4& o) {
-        const float dx = xi.x - o.x, dy = xi.y - o.y, dz = xi.z - o.z;
-        const float r2 = dx * dx + dy * dy + dz * dz;
-        if (r2 <= h2) {
-            const float r = sqrtf(r2);
-            if (r >= 0.0001f) {
-                const float dr = h - r;
-                const float s = (dr * dr / r) * (fi + o.w);
-                fx += dx * s;
-                fy += dy * s;
-                fz += dz * s;
-            }
-        }
-    };
-    if (P.boundary_count) for_each_neighbour(b_cells, c, P, [&](uint32_t j) { body(__ldg(&bpf[j])); });
-    for_each_neighbour(cells, c, P, [&](uint32_t j) { body(__ldg(&pf4[j])); });
+    float3 f = make_float3(0.f, 0.f, 0.f);
+    if (P.boundary_count)
+        for_each_neighbour(b_cells, c, P, [&](uint32_t j) { pressure_force_term(xi, __ldg(&bpf[j]), P.h, P.h2, f); });
+    for_each_neighbour(cells, c, P, [&](uint32_t j) { pressure_force_term(xi, __ldg(&pf4[j]), P.h, P.h2, f); });
     const float m = P.particle_mass;
     const float scale = -P.spiky_d1_norm * m * m;
-    const float3 fp = make_float3(fx * scale, fy * scale, fz * scale);
+    const float3 fp = make_float3(f.x * scale, f.y * scale, f.z * scale);
     f_press[i] = f4(fp, 0.f);
     const bool integrate = mode == 0 ? (ctl->done != 0u) : mode == 2;
     const float3 fo = f3(f_other[i]);

@@ -4,6 +4,7 @@
 // mapping of work to threads differs.
 #include <algorithm>
 
+#include "pair_terms.cuh"
 #include "step_kernels.cuh"
 #include "sweep.cuh"
 
@@ -83,14 +84,7 @@ struct OpNormal {
     __device__ void begin(const DevParams&) const {}
     __device__ void end(const DevParams&, const Result&) const {}
     __device__ __forceinline__ void pair(const DevParams& P, const Self& s, const Cand& o, Acc& a) const {
-        const float dx = s.x - o.x, dy = s.y - o.y, dz = s.z - o.z;
-        const float r2 = dx * dx + dy * dy + dz * dz;
-        if (r2 <= P.h2) {
-            const float k = (r2 - P.h2) * (r2 - P.h2) * __frcp_rn(o.w);
-            a.x += dx * k;
-            a.y += dy * k;
-            a.z += dz * k;
-        }
+        normal_term(s.x, s.y, s.z, o, P.h2, a);
     }
     __device__ Result finish(const DevParams& P, uint32_t i, const Self&, const Acc& a) const {
         const float scale = P.h * P.particle_mass * P.poly6_d1_norm;
@@ -109,9 +103,7 @@ struct ForceSelf {
     float4 xr;
     float3 v, n;
 };
-struct ForceAcc {
-    float3 visc, coh, curv;
-};
+using ForceAcc = ForceAccum;
 struct OpForce {
     using Cand = ForceCand;
     using Self = ForceSelf;
@@ -138,19 +130,7 @@ struct OpForce {
     __device__ void begin(const DevParams&) const {}
     __device__ void end(const DevParams&, const Result&) const {}
     __device__ __forceinline__ void pair(const DevParams& P, const Self& s, const Cand& o, Acc& a) const {
-        const float3 d = make_float3(s.xr.x - o.xr.x, s.xr.y - o.xr.y, s.xr.z - o.xr.z);
-        const float r2 = dot3(d, d);
-        if (r2 <= P.h2) {
-            const float dist = sqrtf(r2);
-            const float rj = o.xr.w;
-            if (rj > 0.0001f) a.visc = a.visc + (f3(o.v) - s.v) * ((P.h - dist) / rj);
-            if (dist > 0.0001f && dist < P.h) {
-                const float corr = 2.f * P.rest_density / (s.xr.w + rj);
-                const float stk = surface_tension_kernel(dist, P.h, P.st_term);
-                a.coh = a.coh + (corr * stk) * (d / dist);
-                a.curv = a.curv + corr * (s.n - f3(o.n));
-            }
-        }
+        force_term(s.xr, s.v, s.n, o.xr, f3(o.v), f3(o.n), P, a);
     }
     __device__ Result finish(const DevParams& P, uint32_t i, const Self& s, const Acc& a) const {
         const float m = P.particle_mass;
@@ -296,18 +276,7 @@ struct OpPressureForce {
     }
     __device__ void end(const DevParams&, const Result&) const {}
     __device__ __forceinline__ void pair(const DevParams& P, const Self& s, const Cand& o, Acc& a) const {
-        const float dx = s.x - o.x, dy = s.y - o.y, dz = s.z - o.z;
-        const float r2 = dx * dx + dy * dy + dz * dz;
-        if (r2 <= P.h2) {
-            const float r = sqrtf(r2);
-            if (r >= 0.0001f) {
-                const float dr = P.h - r;
-                const float k = (dr * dr / r) * (s.w + o.w);
-                a.x += dx * k;
-                a.y += dy * k;
-                a.z += dz * k;
-            }
-        }
+        pressure_force_term(s, o, P.h, P.h2, a);
     }
     __device__ Result finish(const DevParams& P, uint32_t i, const Self& s, const Acc& a) const {
         const float m = P.particle_mass;

@@ -34,7 +34,7 @@ def assert_close(name, got, want, scale=None, rtol=RTOL):
 
 
 def fluid_like(p, min_iters=3, max_iters=7, walls=False, box_lo=(0, 0, 0), box_hi=(0, 0, 0), restitution=0.5,
-               boundary_self_density=0, loop_mode=0, threshold=0.01, kernel_variant=0):
+               boundary_self_density=0, loop_mode=0, threshold=0.01, kernel_variant=2):
     """A context configured through the reference setters for params p (as scene::load does)."""
     f = Fluid(0)
     f.set_delta_t(p.delta_t)

@@ -105,7 +105,7 @@ def _load_case(golden, case, **kw):
     return g, p, f
 
 
-@pytest.mark.parametrize("variant", [0, 1])
+@pytest.mark.parametrize("variant", [0, 1, 2])
 @pytest.mark.parametrize("case", ["step_boundary", "step_fluid"])
 def test_kernel_chain_vs_reference(golden, case, variant):
     g, p, f = _load_case(golden, case, kernel_variant=variant)
@@ -182,7 +182,7 @@ def test_boundary_self_density_computed(golden):
 
 
 @pytest.mark.parametrize("case", ["step_boundary", "step_fluid"])
-@pytest.mark.parametrize("loop_mode,variant", [(0, 0), (1, 0), (0, 1)])
+@pytest.mark.parametrize("loop_mode,variant", [(0, 2), (1, 2), (0, 0), (0, 1)])
 def test_full_steps_vs_reference(golden, case, loop_mode, variant):
     """Fluid::update sequence (min 3 / max 7 iterations, no walls) against the reference's full steps."""
     g, p, f = _load_case(golden, case, loop_mode=loop_mode, kernel_variant=variant)
@@ -203,13 +203,14 @@ def test_full_steps_vs_reference(golden, case, loop_mode, variant):
         k += 1
 
 
-def test_graph_and_host_loop_identical():
+@pytest.mark.parametrize("variant", [0, 2])
+def test_graph_and_host_loop_identical(variant):
     sc = scenes.small_dam(10, seed=3)
     out = []
     for mode in (0, 1):
         f = Fluid(0)
         from pcisph_gb300 import setup_scene
-        setup_scene(f, sc, loop_mode=mode)
+        setup_scene(f, sc, loop_mode=mode, kernel_variant=variant)
         f.step(5)
         st = f.stats()
         out.append((f.get_field("position"), f.get_field("velocity"), f.get_field("pressure"), st.total_iterations))
@@ -221,7 +222,7 @@ def test_graph_and_host_loop_identical():
 # ------------------------------------------------------------------------------------------- full step vs FP64
 
 
-@pytest.mark.parametrize("variant", [0, 1])
+@pytest.mark.parametrize("variant", [0, 1, 2])
 def test_full_step_error_vs_fp64(oracle, variant):
     """One step (fixed 4 iterations, walls on) from identical state: the GPU's error against the FP64 rerun
     is of the order of the FP32 oracle's own error against it."""
@@ -251,7 +252,7 @@ def test_full_step_error_vs_fp64(oracle, variant):
     print({k: f"gpu {a:.1e} / fp32 oracle {b:.1e}" for k, (a, b) in report.items()})
 
 
-@pytest.mark.parametrize("variant", [0, 1])
+@pytest.mark.parametrize("variant", [0, 1, 2])
 def test_long_run_statistics_vs_oracle(oracle, variant):
     """200 steps of a small dam break. SPH trajectories are chaotic: the oracle itself, with one coordinate moved
     by 1 ulp, drifts from its unperturbed run (that drift is measured here). The GPU must stay within 3x that
@@ -357,3 +358,38 @@ def test_setters_zero_velocities_like_the_reference():
         f.update()
         out.append(f.get_field("velocity"))
     np.testing.assert_array_equal(out[0], out[1])
+
+
+def test_list_sweeps_exact_with_fast_particles(oracle):
+    """Neighbour lists (variant 2) drop only pairs that contribute zero, also when some particles move more
+    than half the list skin in one step (those flag their bucket, and particles near a flagged bucket walk
+    the 27 buckets). Against the walking variant (1) and the oracle, from identical state, fixed iterations."""
+    sc = scenes.small_dam(14, seed=9)
+    rng = np.random.default_rng(9)
+    vel = (rng.standard_normal((sc.fluid_count, 3)) * 0.05).astype(np.float32)
+    fast = rng.choice(sc.fluid_count, 25, replace=False)
+    vel[fast] = rng.standard_normal((25, 3)).astype(np.float32) * 8.0  # ~8 m/s: dt |v| >> skin h / 2
+    p = oracle.derive_params(sc.particle_radius, sc.rest_density, sc.fluid_count, 0, sc.delta_t, sc.gravity,
+                             sc.viscosity_constant(), sc.surface_tension)
+    out = {}
+    for variant in (1, 2):
+        f = fluid_like(p, min_iters=5, max_iters=5, walls=True, box_hi=sc.box_hi, kernel_variant=variant)
+        f.set_fluid_state(sc.fluid_pos, vel)
+        f.update()
+        st = f.stats()
+        if variant == 2:
+            assert st.fast_particles > 0 and st.list_fallbacks > 0, (st.fast_particles, st.list_fallbacks)
+        out[variant] = {n: f.get_field(n) for n in ("density", "pressure", "pressure_force", "position",
+                                                    "velocity", "density_variation")}
+    opts = make_options(threshold=0.01, min_iters=5, max_iters=5, walls=True, box_hi=sc.box_hi)
+    s = oracle.new_state(p, sc.fluid_pos, vel)
+    oracle.step(p, opts, s)
+    ref = {"density": s["f_rho"], "pressure": s["f_press"], "pressure_force": s["f_fpress"], "position": s["f_pos"],
+           "velocity": s["f_vel"], "density_variation": s["f_err"]}
+    for n in ref:
+        scale = p.density_variation_scaling_factor * p.rest_density * 5 if n == "pressure" else (
+            p.rest_density if n == "density_variation" else None)
+        e_walk = rel_err(out[1][n], ref[n], scale)
+        e_list = rel_err(out[2][n], ref[n], scale)
+        assert e_list <= max(2 * e_walk, 1e-6), (n, e_list, e_walk)
+        assert rel_err(out[2][n], out[1][n], scale) <= 1e-5, n
