@@ -227,6 +227,55 @@ typedef struct pcisph_kernel_time {
 PCISPH_API int pcisph_profile_enable(pcisph_ctx* ctx, int enable);
 PCISPH_API int pcisph_profile_read(pcisph_ctx* ctx, pcisph_kernel_time* out, int max_entries, int* n_entries);
 
+/* ------------------------------------------------------- batched scenes */
+/* Many independent scenes advanced together: one launch per kernel per step for all of them. Each scene
+ * keeps its own parameters, bucket count and convergence: a scene stops iterating when its own max
+ * density error is below its threshold, while the others continue. Scene ids sit in the high part of one
+ * shared key space (each scene owns a range of buckets), so one stable sort orders all scenes and each
+ * scene's sorted order is the one it would have alone. Scenes have no boundary particles. No counterpart
+ * in the reference, which runs one scene per sim::Fluid. */
+typedef struct pcisph_batch pcisph_batch;
+
+typedef struct pcisph_scene_desc {
+    uint32_t fluid_count;
+    float particle_radius;               /* the reference's setters (Fluid.h:21-29) */
+    float rest_density;
+    float delta_t;
+    float gravity;
+    float viscosity;                     /* the reference's viscosity_constant */
+    float surface_tension;
+    float density_variation_threshold;
+    int32_t min_iterations;
+    int32_t max_iterations;
+    int32_t walls;
+    float box_lo[3];
+    float box_hi[3];
+    float restitution;
+} pcisph_scene_desc;
+
+/* max_particles and max_scenes size the device pool (all of it is allocated here). */
+PCISPH_API int pcisph_batch_create(int device, void* stream, uint32_t max_particles, uint32_t max_scenes,
+                                   pcisph_batch** out);
+PCISPH_API void pcisph_batch_destroy(pcisph_batch* batch);
+/* Bytes of device memory per particle and per scene in a pool (for admission against a budget). */
+PCISPH_API int pcisph_batch_memory_model(uint64_t* bytes_per_particle, uint64_t* bytes_per_scene);
+/* Adds a scene with its initial state (vel may be NULL: zero); *scene_id is a handle valid until removal. */
+PCISPH_API int pcisph_batch_add_scene(pcisph_batch* batch, const pcisph_scene_desc* desc, const float* pos,
+                                      const float* vel, int layout, int memory, int32_t* scene_id);
+/* Removes a scene; the pool is compacted (stream-ordered device copies). */
+PCISPH_API int pcisph_batch_remove_scene(pcisph_batch* batch, int32_t scene_id);
+PCISPH_API int pcisph_batch_info(const pcisph_batch* batch, uint32_t* scenes, uint32_t* particles,
+                                 uint32_t* free_particles);
+/* steps time steps of every scene (one CUDA graph launch each; no host synchronisation). */
+PCISPH_API int pcisph_batch_step(pcisph_batch* batch, uint32_t steps);
+PCISPH_API int pcisph_batch_sync(pcisph_batch* batch);
+/* Synchronises, then reports the scene's last step (and totals since it was added). */
+PCISPH_API int pcisph_batch_scene_stats(pcisph_batch* batch, int32_t scene_id, pcisph_step_stats* out);
+/* A field of one scene (its particles in its own sorted order), as pcisph_get_field. */
+PCISPH_API int pcisph_batch_get_field(pcisph_batch* batch, int32_t scene_id, int field, void* dst,
+                                      size_t dst_bytes, int layout, int memory);
+PCISPH_API uint64_t pcisph_batch_kernel_launches(const pcisph_batch* batch);
+
 /* --------------------------------------------------- standalone kernels */
 /* sort_utils.cl:12-23: key = hash(floor(pos / cell_size)) % bucket_count, id = index. Device pointers. */
 PCISPH_API int pcisph_hash_keys(const pcisph_sim_params* params, const float* pos, int layout, uint32_t count, uint32_t* keys,

@@ -7,4 +7,5 @@ workloads. There is no CPU fallback: without the built library, using the
 step raises.
 """
 from . import scenes  # noqa: F401
+from .batch import Batch  # noqa: F401
 from .fluid import Fluid, RadixSort, default_options, derive_params, hash_keys, setup_scene  # noqa: F401

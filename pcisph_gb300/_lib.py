@@ -59,6 +59,15 @@ class StepStats(C.Structure):
                 ("list_fallbacks", C.c_uint64), ("fast_particles", C.c_uint64)]
 
 
+class SceneDesc(C.Structure):
+    """pcisph_scene_desc: one scene of a batch."""
+    _fields_ = [("fluid_count", C.c_uint32), ("particle_radius", C.c_float), ("rest_density", C.c_float),
+                ("delta_t", C.c_float), ("gravity", C.c_float), ("viscosity", C.c_float),
+                ("surface_tension", C.c_float), ("density_variation_threshold", C.c_float),
+                ("min_iterations", C.c_int32), ("max_iterations", C.c_int32), ("walls", C.c_int32),
+                ("box_lo", C.c_float * 3), ("box_hi", C.c_float * 3), ("restitution", C.c_float)]
+
+
 class KernelTime(C.Structure):
     _fields_ = [("name", C.c_char * 32), ("launches", C.c_uint64), ("total_ms", C.c_double)]
 
@@ -132,6 +141,17 @@ def load():
         "pcisph_radixsort_enqueue": ([vp, vp, vp, sz, C.c_uint, vp], i32),
         "pcisph_radixsort_set_digit_bits": ([vp, i32], i32),
         "pcisph_radixsort_enqueue_noalloc": ([vp, vp, sz, C.c_uint, vp], i32),
+        "pcisph_batch_create": ([i32, vp, u32, u32, C.POINTER(vp)], i32),
+        "pcisph_batch_destroy": ([vp], None),
+        "pcisph_batch_memory_model": ([C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)], i32),
+        "pcisph_batch_add_scene": ([vp, C.POINTER(SceneDesc), vp, vp, i32, i32, C.POINTER(C.c_int32)], i32),
+        "pcisph_batch_remove_scene": ([vp, C.c_int32], i32),
+        "pcisph_batch_info": ([vp, C.POINTER(u32), C.POINTER(u32), C.POINTER(u32)], i32),
+        "pcisph_batch_step": ([vp, u32], i32),
+        "pcisph_batch_sync": ([vp], i32),
+        "pcisph_batch_scene_stats": ([vp, C.c_int32, C.POINTER(StepStats)], i32),
+        "pcisph_batch_get_field": ([vp, C.c_int32, i32, vp, sz, i32, i32], i32),
+        "pcisph_batch_kernel_launches": ([vp], C.c_uint64),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)

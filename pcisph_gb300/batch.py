@@ -1,0 +1,103 @@
+"""Many independent scenes advanced together (the pcisph_batch_* C ABI).
+
+One launch per kernel per time step serves every scene; each scene keeps its own parameters and its own
+convergence (it stops iterating when its own max density error is below its threshold). A scene's result
+is the one it would have alone (tests/test_gpu_batch.py).
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from ._lib import FIELDS, SceneDesc, StepStats, UINT_FIELDS, VECTOR_FIELDS, check, load
+
+
+def scene_desc(scene, min_iters=None, max_iters=None):
+    """pcisph_scene_desc for a scenes.Scene."""
+    d = SceneDesc()
+    d.fluid_count = scene.fluid_count
+    d.particle_radius = scene.particle_radius
+    d.rest_density = scene.rest_density
+    d.delta_t = scene.delta_t
+    d.gravity = scene.gravity
+    d.viscosity = scene.viscosity_constant()
+    d.surface_tension = scene.surface_tension
+    d.density_variation_threshold = scene.threshold
+    d.min_iterations = scene.min_iters if min_iters is None else min_iters
+    d.max_iterations = scene.max_iters if max_iters is None else max_iters
+    d.walls = int(scene.walls)
+    d.box_lo[:] = [float(v) for v in scene.box_lo]
+    d.box_hi[:] = [float(v) for v in scene.box_hi]
+    d.restitution = scene.restitution
+    return d
+
+
+def memory_model():
+    """(bytes per particle, bytes per scene) of a batch pool."""
+    a, b = C.c_uint64(), C.c_uint64()
+    check(load().pcisph_batch_memory_model(C.byref(a), C.byref(b)))
+    return a.value, b.value
+
+
+class Batch:
+    def __init__(self, device=0, max_particles=1 << 20, max_scenes=256, stream=None):
+        L = load()
+        h = C.c_void_p()
+        check(L.pcisph_batch_create(int(device), C.c_void_p(stream) if stream else None, int(max_particles),
+                                    int(max_scenes), C.byref(h)))
+        self._h, self._L = h, L
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.pcisph_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def add_scene(self, scene, min_iters=None, max_iters=None, pos=None, vel=None):
+        d = scene_desc(scene, min_iters, max_iters)
+        pos = np.ascontiguousarray(scene.fluid_pos if pos is None else pos, np.float32)
+        vel = scene.fluid_vel if vel is None else vel
+        vel = None if vel is None else np.ascontiguousarray(vel, np.float32)
+        sid = C.c_int32()
+        layout = _lib.LAYOUT_FLOAT4 if pos.shape[1] == 4 else _lib.LAYOUT_PACKED3
+        check(self._L.pcisph_batch_add_scene(self._h, C.byref(d), C.c_void_p(pos.ctypes.data),
+                                             None if vel is None else C.c_void_p(vel.ctypes.data), layout,
+                                             _lib.MEM_HOST, C.byref(sid)))
+        return sid.value
+
+    def remove_scene(self, sid):
+        check(self._L.pcisph_batch_remove_scene(self._h, int(sid)))
+
+    def info(self):
+        a, b, c = C.c_uint32(), C.c_uint32(), C.c_uint32()
+        check(self._L.pcisph_batch_info(self._h, C.byref(a), C.byref(b), C.byref(c)))
+        return a.value, b.value, c.value
+
+    def step(self, n=1):
+        check(self._L.pcisph_batch_step(self._h, int(n)))
+
+    def sync(self):
+        check(self._L.pcisph_batch_sync(self._h))
+
+    def stats(self, sid):
+        s = StepStats()
+        check(self._L.pcisph_batch_scene_stats(self._h, int(sid), C.byref(s)))
+        return s
+
+    def kernel_launches(self):
+        return int(self._L.pcisph_batch_kernel_launches(self._h))
+
+    def get_field(self, sid, name, count, layout="packed3"):
+        if name in VECTOR_FIELDS:
+            lay = _lib.LAYOUT_PACKED3 if layout == "packed3" else _lib.LAYOUT_FLOAT4
+            out = np.empty((count, 3 if lay == _lib.LAYOUT_PACKED3 else 4), np.float32)
+        else:
+            lay, out = _lib.LAYOUT_SCALAR, np.empty(count, np.uint32 if name in UINT_FIELDS else np.float32)
+        check(self._L.pcisph_batch_get_field(self._h, int(sid), FIELDS[name], C.c_void_p(out.ctypes.data),
+                                             out.nbytes, lay, _lib.MEM_HOST))
+        return out

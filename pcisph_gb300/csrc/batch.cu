@@ -1,0 +1,481 @@
+// batch.cu -- many independent scenes advanced by one set of launches (C ABI in include/pcisph_gpu.h).
+//
+// Layout. The scenes share one particle pool: scene k occupies [offset_k, offset_k + N_k) of every
+// per-particle array, scenes packed in insertion order, compacted on removal. Scene k owns the bucket
+// range [bucket_base_k, bucket_base_k + bucket_count_k) of one cell table, and its key for a particle is
+// bucket_base_k + the reference key (grid_utils.cl:12-19 with the scene's own bucket_count). The keys of
+// scene k are therefore all below those of scene k+1: one stable radix sort of the whole pool leaves
+// every scene in its own range, ordered as a sort of that scene alone would order it.
+//
+// Step. One CUDA graph per batch composition: begin, clear tables, hash, sort, reorder, then the list
+// sweeps of list_kernels.cu with per-particle parameters from the scene table, and a conditional WHILE
+// node over {pressure, per-scene decision, pressure force}. A scene's decision follows the reference
+// (Fluid.cpp:284-306) with its own threshold and limits; a converged scene integrates and then idles
+// (its particles skip the sweeps) while the others keep iterating; the loop ends when every scene is done.
+#include <cuda_runtime.h>
+
+#include <cstring>
+#include <vector>
+
+#include "host_util.h"
+#include "list_kernels.cuh"
+#include "radix_sort.cuh"
+#include "step_kernels.cuh"
+
+using namespace pcisph;
+using namespace pcisph::host;
+
+namespace {
+
+#define BTRY(call)                                                                                             \
+    do {                                                                                                       \
+        cudaError_t e_ = (call);                                                                               \
+        if (e_ != cudaSuccess) return report_error(PCISPH_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+struct SceneSlot {
+    int32_t id;
+    pcisph_scene_desc desc;
+    pcisph_sim_params params;
+    uint32_t offset, count, bucket_base;
+};
+
+constexpr size_t kParticleBytes = 10 * 16 + 3 * 4 + 2 * 4 + 2 + kListCap * 4 + 4 + 16;  // arrays + staging
+constexpr size_t kBucketBytesPerParticle = 5;  // (8 B table + 1 B flag) per bucket, ~N/2 buckets
+
+}  // namespace
+
+struct pcisph_batch {
+    int device = 0;
+    cudaStream_t user_stream = nullptr, own_stream = nullptr, capture_stream = nullptr;
+    uint32_t max_particles = 0, max_scenes = 0, max_buckets = 0;
+    DeviceBlock pool, tables;
+    float4 *state_pos, *state_vel, *pos, *vel, *pr4, *normal, *f_other, *f_press, *pred, *pf4, *staging;
+    float *rho, *press, *err;
+    uint32_t *keys, *ids, *nbr, *nbr_count;
+    uint16_t* scene_of;
+    uint2* cells;
+    unsigned char* bucket_fast;
+    DevParams* d_table;
+    Control* d_ctls;
+    uint32_t* d_offsets;
+    Control* d_batch;
+    Control* h_ctls = nullptr;  // pinned
+    RadixSorter sorter;
+    DeviceBlock sort_block;
+    std::vector<SceneSlot> scenes;
+    int32_t next_id = 1;
+    uint32_t n_particles = 0, n_buckets = 0;
+    int max_iters = 1;
+    cudaGraphExec_t graph_exec = nullptr;
+    bool graph_valid = false;
+    uint64_t host_launches = 0;
+    int prefix_launches = 0, iter_launches = 3;
+    uint32_t *sorted_keys = nullptr, *sorted_ids = nullptr;
+
+    cudaStream_t stream() const { return user_stream; }
+
+    ~pcisph_batch() {
+        DeviceGuard g(device);
+        if (user_stream) cudaStreamSynchronize(user_stream);
+        if (graph_exec) cudaGraphExecDestroy(graph_exec);
+        pool.release();
+        tables.release();
+        sort_block.release();
+        if (h_ctls) cudaFreeHost(h_ctls);
+        if (own_stream) cudaStreamDestroy(own_stream);
+        if (capture_stream) cudaStreamDestroy(capture_stream);
+    }
+
+    int allocate() {
+        const size_t n = max_particles, nb = max_buckets, ns = max_scenes;
+        const size_t bytes = 11 * align256(n * 16) + 3 * align256(n * 4) + 4 * align256(n * 4) + align256(n * 2) +
+                             align256(n * kListCap * 4) + align256(nb * 8) + align256(nb);
+        if (pool.ensure(bytes) != cudaSuccess)
+            return report_error(PCISPH_ERR_OOM, "device allocation of the batch pool failed (" + std::to_string(bytes) + " bytes)");
+        Carver c{static_cast<unsigned char*>(pool.p)};
+        state_pos = c.take<float4>(n);
+        state_vel = c.take<float4>(n);
+        pos = c.take<float4>(n);
+        vel = c.take<float4>(n);
+        pr4 = c.take<float4>(n);
+        normal = c.take<float4>(n);
+        f_other = c.take<float4>(n);
+        f_press = c.take<float4>(n);
+        pred = c.take<float4>(n);
+        pf4 = c.take<float4>(n);
+        staging = c.take<float4>(n);
+        rho = c.take<float>(n);
+        press = c.take<float>(n);
+        err = c.take<float>(n);
+        keys = c.take<uint32_t>(n);
+        ids = c.take<uint32_t>(n);
+        nbr_count = c.take<uint32_t>(n);
+        c.take<uint32_t>(n);
+        scene_of = c.take<uint16_t>(n);
+        nbr = c.take<uint32_t>(n * kListCap);
+        cells = c.take<uint2>(nb);
+        bucket_fast = c.take<unsigned char>(nb);
+        const size_t tbytes = align256(ns * sizeof(DevParams)) + align256(ns * sizeof(Control)) +
+                              align256((ns + 1) * 4) + align256(sizeof(Control));
+        if (tables.ensure(tbytes) != cudaSuccess) return report_error(PCISPH_ERR_OOM, "device allocation of the scene tables failed");
+        Carver t{static_cast<unsigned char*>(tables.p)};
+        d_table = t.take<DevParams>(ns);
+        d_ctls = t.take<Control>(ns);
+        d_offsets = t.take<uint32_t>(ns + 1);
+        d_batch = t.take<Control>(1);
+        BTRY(cudaMemset(tables.p, 0, tbytes));
+        const size_t sbytes = RadixSorter::scratch_bytes(n, sorter.digit_bits());
+        if (sort_block.ensure(sbytes) != cudaSuccess) return report_error(PCISPH_ERR_OOM, "device allocation of the sort scratch failed");
+        sorter.set_scratch(sort_block.p, sort_block.cap);
+        BTRY(cudaMallocHost(&h_ctls, ns * sizeof(Control)));
+        return PCISPH_OK;
+    }
+
+    SceneTable scene_table() const {
+        return SceneTable{d_table, d_ctls, scene_of, n_particles, (uint32_t)scenes.size()};
+    }
+    ListBuffers list_buffers() const {
+        return ListBuffers{pos, vel, pr4, normal, f_other, f_press, pred, pf4, state_pos, state_vel, rho, press, err,
+                           cells, cells, nullptr, nullptr, nbr, nbr_count, bucket_fast};
+    }
+
+    // Scene tables after a change of composition: bucket ranges, parameters, offsets, particle -> scene.
+    int rebuild() {
+        std::vector<DevParams> table(scenes.size());
+        std::vector<uint32_t> offsets(scenes.size() + 1);
+        uint32_t base = 0, off = 0;
+        max_iters = 1;
+        for (size_t k = 0; k < scenes.size(); ++k) {
+            SceneSlot& s = scenes[k];
+            s.offset = off;
+            s.bucket_base = base;
+            const pcisph_scene_desc& d = s.desc;
+            make_devparams(s.params, d.min_iterations, d.max_iterations, d.walls, d.box_lo, d.box_hi, d.restitution,
+                           d.density_variation_threshold, 0.25f, base, &table[k]);
+            offsets[k] = off;
+            off += s.count;
+            base += s.params.bucket_count;
+            max_iters = std::max(max_iters, d.max_iterations);
+        }
+        offsets[scenes.size()] = off;
+        n_particles = off;
+        n_buckets = base;
+        cudaStream_t st = stream();
+        if (!scenes.empty()) {
+            BTRY(cudaMemcpyAsync(d_table, table.data(), table.size() * sizeof(DevParams), cudaMemcpyHostToDevice, st));
+            BTRY(cudaMemcpyAsync(d_offsets, offsets.data(), offsets.size() * 4, cudaMemcpyHostToDevice, st));
+            launch_scene_of(d_offsets, (uint32_t)scenes.size(), n_particles, scene_of, st);
+            ++host_launches;
+            BTRY(cudaGetLastError());
+        }
+        BTRY(cudaStreamSynchronize(st));  // the host vectors above go out of scope
+        graph_valid = false;
+        return PCISPH_OK;
+    }
+
+    int record_prefix(cudaStream_t s) {
+        const SceneTable t = scene_table();
+        int nl = 0;
+        launch_batch_begin(d_ctls, t.n_scenes, d_batch, s);
+        ++nl;
+        if (cudaMemsetAsync(cells, 0, (size_t)n_buckets * 8, s) != cudaSuccess) return -1;
+        if (cudaMemsetAsync(bucket_fast, 0, n_buckets, s) != cudaSuccess) return -1;
+        launch_hash_scenes(t, state_pos, keys, s);
+        ++nl;
+        uint32_t *sk = nullptr, *sv = nullptr;
+        if (sorter.sort(keys, ids, n_particles, key_bits(n_buckets), true, s, &sk, &sv) != cudaSuccess) return -1;
+        nl += sorter.last_launches();
+        sorted_keys = sk;
+        sorted_ids = sv;
+        DevParams R{};
+        R.bucket_count = n_buckets;
+        launch_reorder(sk, sv, state_pos, state_vel, n_particles, pos, vel, cells, nullptr, nullptr, R, d_batch, s);
+        const ListBuffers b = list_buffers();
+        launch_density_scenes(t, b, s);
+        launch_normal_scenes(t, b, s);
+        launch_force_scenes(t, b, s);
+        nl += 4;
+        return cudaGetLastError() == cudaSuccess ? nl : -1;
+    }
+
+    int build_graph() {
+        if (graph_exec) {
+            cudaGraphExecDestroy(graph_exec);
+            graph_exec = nullptr;
+        }
+        cudaStream_t s = capture_stream;
+        cudaGraph_t graph = nullptr;
+        BTRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        const int nl = record_prefix(s);
+        cudaStreamCaptureStatus st;
+        const cudaGraphNode_t* deps = nullptr;
+        size_t ndeps = 0;
+        cudaError_t e = cudaStreamGetCaptureInfo(s, &st, nullptr, nullptr, &deps, nullptr, &ndeps);
+        std::vector<cudaGraphNode_t> leaves(deps, deps + (e == cudaSuccess ? ndeps : 0));
+        cudaError_t e2 = cudaStreamEndCapture(s, &graph);
+        if (nl < 0 || e != cudaSuccess || e2 != cudaSuccess) {
+            if (graph) cudaGraphDestroy(graph);
+            return report_error(PCISPH_ERR_CUDA, std::string("graph capture of the batch step failed: ") +
+                                                     cudaGetErrorString(e != cudaSuccess ? e : e2));
+        }
+        prefix_launches = nl;
+        cudaGraphConditionalHandle handle;
+        BTRY(cudaGraphConditionalHandleCreate(&handle, graph, 1, cudaGraphCondAssignDefault));
+        cudaGraphNodeParams cp{};
+        cp.type = cudaGraphNodeTypeConditional;
+        cp.conditional.handle = handle;
+        cp.conditional.type = cudaGraphCondTypeWhile;
+        cp.conditional.size = 1;
+        cudaGraphNode_t loop_node;
+        BTRY(cudaGraphAddNode(&loop_node, graph, leaves.data(), nullptr, leaves.size(), &cp));
+        BTRY(cudaStreamBeginCaptureToGraph(s, cp.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                           cudaStreamCaptureModeThreadLocal));
+        const SceneTable t = scene_table();
+        const ListBuffers b = list_buffers();
+        launch_pressure_scenes(t, b, s);
+        launch_batch_decide(t, d_batch, max_iters, handle, true, s);
+        launch_pressure_force_scenes(t, b, s);
+        cudaGraph_t body = nullptr;
+        BTRY(cudaStreamEndCapture(s, &body));
+        e = cudaGraphInstantiate(&graph_exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) return report_error(PCISPH_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+        graph_valid = true;
+        return PCISPH_OK;
+    }
+
+    int step(uint32_t steps) {
+        if (scenes.empty()) return PCISPH_OK;
+        if (!graph_valid) {
+            int rc = build_graph();
+            if (rc) return rc;
+        }
+        for (uint32_t k = 0; k < steps; ++k) {
+            BTRY(cudaGraphLaunch(graph_exec, stream()));
+            host_launches += prefix_launches;
+        }
+        return PCISPH_OK;
+    }
+
+    int find(int32_t id) const {
+        for (size_t k = 0; k < scenes.size(); ++k)
+            if (scenes[k].id == id) return (int)k;
+        return -1;
+    }
+
+    int copy_in(float4* dst, const float* src, uint32_t n, int layout, int memory) {
+        if (!n) return PCISPH_OK;
+        cudaStream_t s = stream();
+        const cudaMemcpyKind kind = memory == PCISPH_MEM_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
+        if (layout == PCISPH_LAYOUT_FLOAT4) {
+            BTRY(cudaMemcpyAsync(dst, src, (size_t)n * 16, kind, s));
+        } else {
+            const float* d = src;
+            if (memory == PCISPH_MEM_HOST) {
+                BTRY(cudaMemcpyAsync(staging, src, (size_t)n * 12, kind, s));
+                d = reinterpret_cast<const float*>(staging);
+            }
+            launch_pack3_to4(d, dst, n, s);
+            ++host_launches;
+            BTRY(cudaGetLastError());
+            if (memory == PCISPH_MEM_HOST) BTRY(cudaStreamSynchronize(s));  // staging is reused
+        }
+        return PCISPH_OK;
+    }
+};
+
+extern "C" {
+
+int pcisph_batch_memory_model(uint64_t* bytes_per_particle, uint64_t* bytes_per_scene) {
+    if (bytes_per_particle) *bytes_per_particle = kParticleBytes + kBucketBytesPerParticle + 48;  // + sort scratch
+    if (bytes_per_scene) *bytes_per_scene = sizeof(DevParams) + sizeof(Control) + 4 + 64 * 9;
+    return PCISPH_OK;
+}
+
+int pcisph_batch_create(int device, void* stream, uint32_t max_particles, uint32_t max_scenes, pcisph_batch** out) {
+    if (!out) return report_error(PCISPH_ERR_INVALID_ARG, "out is NULL");
+    *out = nullptr;
+    if (max_particles == 0 || max_scenes == 0 || max_scenes > 65535)
+        return report_error(PCISPH_ERR_INVALID_ARG, "max_particles must be > 0 and max_scenes in 1..65535");
+    int ndev = 0;
+    BTRY(cudaGetDeviceCount(&ndev));
+    if (device < 0 || device >= ndev) return report_error(PCISPH_ERR_INVALID_ARG, "no CUDA device " + std::to_string(device));
+    DeviceGuard g(device);
+    BTRY(cudaFree(nullptr));
+    BTRY(radix_configure_kernels());
+    pcisph_batch* b = new pcisph_batch();
+    b->device = device;
+    b->max_particles = max_particles;
+    b->max_scenes = max_scenes;
+    b->max_buckets = max_particles / 2 + 64u * max_scenes;
+    cudaError_t e = cudaStreamCreateWithFlags(&b->capture_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->own_stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        delete b;
+        return report_error(PCISPH_ERR_CUDA, std::string("stream creation: ") + cudaGetErrorString(e));
+    }
+    b->user_stream = stream ? static_cast<cudaStream_t>(stream) : b->own_stream;
+    int rc = b->allocate();
+    if (rc) {
+        delete b;
+        return rc;
+    }
+    *out = b;
+    return PCISPH_OK;
+}
+
+void pcisph_batch_destroy(pcisph_batch* b) { delete b; }
+
+int pcisph_batch_add_scene(pcisph_batch* b, const pcisph_scene_desc* d, const float* pos, const float* vel,
+                           int layout, int memory, int32_t* scene_id) {
+    if (!b || !d || !scene_id) return report_error(PCISPH_ERR_INVALID_ARG, "NULL argument");
+    if (d->fluid_count == 0 || !pos) return report_error(PCISPH_ERR_INVALID_ARG, "a scene needs particles");
+    if (layout != PCISPH_LAYOUT_PACKED3 && layout != PCISPH_LAYOUT_FLOAT4)
+        return report_error(PCISPH_ERR_INVALID_ARG, "positions take PACKED3 or FLOAT4");
+    if (d->min_iterations < 1 || d->max_iterations < 1 || d->max_iterations > 10000)
+        return report_error(PCISPH_ERR_INVALID_ARG, "iteration limits must be in 1..10000");
+    if (b->scenes.size() >= b->max_scenes) return report_error(PCISPH_ERR_OOM, "batch is full (max_scenes)");
+    if ((uint64_t)b->n_particles + d->fluid_count > b->max_particles)
+        return report_error(PCISPH_ERR_OOM, "batch is full (max_particles)");
+    DeviceGuard g(b->device);
+    SceneSlot s{};
+    s.id = b->next_id++;
+    s.desc = *d;
+    s.count = d->fluid_count;
+    pcisph_derive_params(d->particle_radius, d->rest_density, d->fluid_count, 0, d->delta_t, d->gravity, d->viscosity,
+                         d->surface_tension, &s.params);
+    if ((uint64_t)b->n_buckets + s.params.bucket_count > b->max_buckets)
+        return report_error(PCISPH_ERR_OOM, "batch is full (buckets)");
+    const uint32_t off = b->n_particles;
+    int rc = b->copy_in(b->state_pos + off, pos, s.count, layout, memory);
+    if (!rc && vel) rc = b->copy_in(b->state_vel + off, vel, s.count, layout, memory);
+    else if (!rc) BTRY(cudaMemsetAsync(b->state_vel + off, 0, (size_t)s.count * 16, b->stream()));
+    if (rc) return rc;
+    const size_t k = b->scenes.size();
+    BTRY(cudaMemsetAsync(b->d_ctls + k, 0, sizeof(Control), b->stream()));
+    b->scenes.push_back(s);
+    rc = b->rebuild();
+    if (rc) return rc;
+    *scene_id = s.id;
+    return PCISPH_OK;
+}
+
+int pcisph_batch_remove_scene(pcisph_batch* b, int32_t id) {
+    if (!b) return report_error(PCISPH_ERR_INVALID_ARG, "batch is NULL");
+    const int k = b->find(id);
+    if (k < 0) return report_error(PCISPH_ERR_INVALID_ARG, "unknown scene id " + std::to_string(id));
+    DeviceGuard g(b->device);
+    cudaStream_t s = b->stream();
+    const SceneSlot gone = b->scenes[k];
+    const uint32_t tail = gone.offset + gone.count, tail_n = b->n_particles - tail;
+    if (tail_n) {  // move the later scenes down through scratch arrays (the ranges may overlap)
+        BTRY(cudaMemcpyAsync(b->pos, b->state_pos + tail, (size_t)tail_n * 16, cudaMemcpyDeviceToDevice, s));
+        BTRY(cudaMemcpyAsync(b->vel, b->state_vel + tail, (size_t)tail_n * 16, cudaMemcpyDeviceToDevice, s));
+        BTRY(cudaMemcpyAsync(b->state_pos + gone.offset, b->pos, (size_t)tail_n * 16, cudaMemcpyDeviceToDevice, s));
+        BTRY(cudaMemcpyAsync(b->state_vel + gone.offset, b->vel, (size_t)tail_n * 16, cudaMemcpyDeviceToDevice, s));
+    }
+    const size_t later = b->scenes.size() - (size_t)k - 1;
+    if (later) {  // per-scene statistics move with their scenes
+        BTRY(cudaMemcpyAsync(b->h_ctls, b->d_ctls + k + 1, later * sizeof(Control), cudaMemcpyDeviceToHost, s));
+        BTRY(cudaStreamSynchronize(s));
+        BTRY(cudaMemcpyAsync(b->d_ctls + k, b->h_ctls, later * sizeof(Control), cudaMemcpyHostToDevice, s));
+    }
+    b->scenes.erase(b->scenes.begin() + k);
+    return b->rebuild();
+}
+
+int pcisph_batch_info(const pcisph_batch* b, uint32_t* scenes, uint32_t* particles, uint32_t* free_particles) {
+    if (!b) return report_error(PCISPH_ERR_INVALID_ARG, "batch is NULL");
+    if (scenes) *scenes = (uint32_t)b->scenes.size();
+    if (particles) *particles = b->n_particles;
+    if (free_particles) *free_particles = b->max_particles - b->n_particles;
+    return PCISPH_OK;
+}
+
+int pcisph_batch_step(pcisph_batch* b, uint32_t steps) {
+    if (!b) return report_error(PCISPH_ERR_INVALID_ARG, "batch is NULL");
+    DeviceGuard g(b->device);
+    return b->step(steps);
+}
+
+int pcisph_batch_sync(pcisph_batch* b) {
+    if (!b) return report_error(PCISPH_ERR_INVALID_ARG, "batch is NULL");
+    DeviceGuard g(b->device);
+    BTRY(cudaStreamSynchronize(b->stream()));
+    return PCISPH_OK;
+}
+
+int pcisph_batch_scene_stats(pcisph_batch* b, int32_t id, pcisph_step_stats* out) {
+    if (!b || !out) return report_error(PCISPH_ERR_INVALID_ARG, "NULL argument");
+    const int k = b->find(id);
+    if (k < 0) return report_error(PCISPH_ERR_INVALID_ARG, "unknown scene id " + std::to_string(id));
+    DeviceGuard g(b->device);
+    BTRY(cudaStreamSynchronize(b->stream()));
+    Control c{}, all{};
+    BTRY(cudaMemcpy(&c, b->d_ctls + k, sizeof(Control), cudaMemcpyDeviceToHost));
+    BTRY(cudaMemcpy(&all, b->d_batch, sizeof(Control), cudaMemcpyDeviceToHost));
+    c.status |= all.status & 4u;  // a broken sort concerns every scene of the step
+    c.status_all |= c.status;
+    out->iterations = c.iterations_last;
+    out->max_density_error = c.max_err_last;
+    out->status = c.status;
+    out->status_all = c.status_all;
+    out->steps = c.steps;
+    out->total_iterations = c.total_iters;
+    out->list_fallbacks = c.list_fallbacks;
+    out->fast_particles = c.fast_particles;
+    return PCISPH_OK;
+}
+
+int pcisph_batch_get_field(pcisph_batch* b, int32_t id, int field, void* dst, size_t dst_bytes, int layout,
+                           int memory) {
+    if (!b) return report_error(PCISPH_ERR_INVALID_ARG, "batch is NULL");
+    const int k = b->find(id);
+    if (k < 0) return report_error(PCISPH_ERR_INVALID_ARG, "unknown scene id " + std::to_string(id));
+    const SceneSlot& s = b->scenes[k];
+    const void* src = nullptr;
+    bool vec = true;
+    switch (field) {
+        case PCISPH_FIELD_POSITION: src = b->state_pos + s.offset; break;
+        case PCISPH_FIELD_VELOCITY: src = b->state_vel + s.offset; break;
+        case PCISPH_FIELD_NORMAL: src = b->normal + s.offset; break;
+        case PCISPH_FIELD_PREDICTED_POSITION: src = b->pred + s.offset; break;
+        case PCISPH_FIELD_OTHER_FORCE: src = b->f_other + s.offset; break;
+        case PCISPH_FIELD_PRESSURE_FORCE: src = b->f_press + s.offset; break;
+        case PCISPH_FIELD_SORTED_POSITION: src = b->pos + s.offset; break;
+        case PCISPH_FIELD_DENSITY: src = b->rho + s.offset; vec = false; break;
+        case PCISPH_FIELD_PRESSURE: src = b->press + s.offset; vec = false; break;
+        case PCISPH_FIELD_DENSITY_VARIATION: src = b->err + s.offset; vec = false; break;
+        default: return report_error(PCISPH_ERR_INVALID_ARG, "field not available for batched scenes");
+    }
+    if (vec && layout == PCISPH_LAYOUT_SCALAR) return report_error(PCISPH_ERR_INVALID_ARG, "vector field: use PACKED3 or FLOAT4");
+    if (!vec && layout != PCISPH_LAYOUT_SCALAR) return report_error(PCISPH_ERR_INVALID_ARG, "scalar field: use SCALAR");
+    const size_t need = (size_t)s.count * (layout == PCISPH_LAYOUT_PACKED3 ? 12 : layout == PCISPH_LAYOUT_FLOAT4 ? 16 : 4);
+    if (!dst || dst_bytes < need) return report_error(PCISPH_ERR_INVALID_ARG, "destination too small");
+    DeviceGuard g(b->device);
+    cudaStream_t st = b->stream();
+    const cudaMemcpyKind kind = memory == PCISPH_MEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+    if (layout == PCISPH_LAYOUT_PACKED3) {
+        float* o = memory == PCISPH_MEM_HOST ? reinterpret_cast<float*>(b->staging) : static_cast<float*>(dst);
+        launch_unpack4_to3(static_cast<const float4*>(src), o, s.count, st);
+        ++b->host_launches;
+        BTRY(cudaGetLastError());
+        if (memory == PCISPH_MEM_HOST) BTRY(cudaMemcpyAsync(dst, o, need, kind, st));
+    } else {
+        BTRY(cudaMemcpyAsync(dst, src, need, kind, st));
+    }
+    if (memory == PCISPH_MEM_HOST) BTRY(cudaStreamSynchronize(st));
+    return PCISPH_OK;
+}
+
+uint64_t pcisph_batch_kernel_launches(const pcisph_batch* b) {
+    if (!b) return 0;
+    DeviceGuard g(b->device);
+    cudaStreamSynchronize(b->user_stream);
+    Control c{};
+    cudaMemcpy(&c, b->d_batch, sizeof(Control), cudaMemcpyDeviceToHost);
+    return b->host_launches + c.total_iters * (uint64_t)b->iter_launches;
+}
+
+}  // extern "C"

@@ -23,6 +23,8 @@ struct DevParams {
     uint32_t fluid_count, boundary_count, bucket_count;
     // modulo by bucket_count
     uint32_t bk_magic, bk_shift;
+    // first entry of this scene's buckets in a cell table shared by several scenes (0 for one scene)
+    uint32_t bucket_base;
     // neighbour lists (kernel_variant 2): capacity per particle, radius h (1 + skin) and its square
     uint32_t list_cap;
     float list_r, list_r2, list_half_skin;
@@ -47,6 +49,8 @@ struct Control {
     unsigned int max_disp_bits;  // float bits of max |x* - x| this step (neighbour-list validity)
     unsigned long long list_fallbacks;  // pressure sweeps in which some particle moved more than skin / 2
     unsigned long long fast_particles;  // predictions that moved more than skin / 2 (each flags its bucket)
+    unsigned int finished;       // batched scenes: the step is complete (no more corrective iterations)
+    unsigned int any_running;    // batch control: some scene still iterates
 };
 
 __host__ __device__ inline void magic_for(uint32_t d, uint32_t* magic, uint32_t* shift) {
@@ -103,7 +107,7 @@ __device__ __forceinline__ void for_each_neighbour(const uint2* __restrict__ cel
             for (int dx = -1; dx <= 1; ++dx) {
                 const uint32_t x = c.x + (uint32_t)dx;
                 const uint32_t v = (((x * 19349663u) ^ hyz) << 6) + (x & 63u) + lyz;
-                const uint2 r = __ldg(&cells[mod_bk(v & 0x7FFFFFFFu, P)]);
+                const uint2 r = __ldg(&cells[P.bucket_base + mod_bk(v & 0x7FFFFFFFu, P)]);
                 for (uint32_t j = r.x; j < r.y; ++j) body(j);
             }
         }

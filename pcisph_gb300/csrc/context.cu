@@ -24,10 +24,13 @@
 #include "../../include/pcisph_gpu.h"
 #include "common.cuh"
 #include "radix_sort.cuh"
+#include "host_util.h"
+#include "list_kernels.cuh"
 #include "step_kernels.cuh"
 #include "sweep.cuh"
 
 using namespace pcisph;
+using namespace pcisph::host;
 
 namespace {
 
@@ -43,111 +46,6 @@ int fail(int code, const std::string& msg) {
         cudaError_t e_ = (call);                                                                      \
         if (e_ != cudaSuccess) return fail(PCISPH_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
     } while (0)
-
-size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
-
-const float kPi = 3.14159265358979323846f;  // utils/constants.h:4
-constexpr uint32_t kListCap = 96;           // neighbour-list entries per particle (multiple of 4)
-
-// Fluid.cpp:125-133
-uint32_t sort_bit_count_ref(uint32_t elements) {
-    uint32_t max_value = 0;
-    for (int i = 0; i < 32; i++) {
-        max_value = (max_value << 1) | 1u;
-        if (max_value >= elements - 1u) return (uint32_t)(i + 1);
-    }
-    return 32u;
-}
-
-// Bits needed for keys < bucket_count.
-int key_bits(uint32_t bucket_count) {
-    int b = 1;
-    while (b < 32 && (1ull << b) < (unsigned long long)bucket_count) ++b;
-    return b;
-}
-
-// update_deduced_attributes (Fluid.cpp:377-443): the same expressions, so the same floats.
-void derive(pcisph_sim_params* p) {
-    p->kernel_radius = 4.f * p->particle_radius;
-    p->kernel_radius2 = std::pow(p->kernel_radius, 2.f);
-    p->particle_mass = (float)((double)p->rest_density / std::pow((double)(1.f / (2.f * p->particle_radius)), 3.0));
-    p->bucket_count = p->fluid_count / 2;
-    p->bucket_count -= p->bucket_count % 64;
-    p->bucket_count = std::max(64u, p->bucket_count);
-    p->cell_size = p->kernel_radius;
-    p->poly6_normalization = 315.f / (64.f * kPi * std::pow(p->kernel_radius, 9.f));
-    p->poly6_d1_normalization = -945.f / (32.f * kPi * std::pow(p->kernel_radius, 9.f));
-    p->viscosity_d2_normalization = 45.f / (kPi * std::pow(p->kernel_radius, 6.0f));
-    p->spiky_d1_normalization = -45.f / (kPi * std::pow(p->kernel_radius, 6.0f));
-    p->surface_tension_normalization = 32.f / (kPi * std::pow(p->kernel_radius, 9.f));
-    p->surface_tension_term = std::pow(p->kernel_radius, 6.f) / 64.f;
-    const float particle_size = 2.f * p->particle_radius;
-    const float beta = p->delta_t * p->delta_t * p->particle_mass * p->particle_mass * 2.f /
-                       (p->rest_density * p->rest_density);
-    float sum[3] = {0.f, 0.f, 0.f}, sum_sq = 0.f;
-    const float lim = p->kernel_radius + particle_size;
-    for (float z = -p->kernel_radius - particle_size; z <= lim; z += 2.f * p->particle_radius)
-        for (float y = -p->kernel_radius - particle_size; y <= lim; y += 2.f * p->particle_radius)
-            for (float x = -p->kernel_radius - particle_size; x <= lim; x += 2.f * p->particle_radius) {
-                const float r = std::sqrt(x * x + y * y + z * z);
-                const float r2 = r * r;
-                if (r2 < p->kernel_radius2) {
-                    const float f = (float)((double)p->poly6_d1_normalization *
-                                            std::pow((double)(p->kernel_radius2 - r2), 2.0));
-                    const float v[3] = {-f * x, -f * y, -f * z};
-                    for (int i = 0; i < 3; i++) {
-                        sum[i] += v[i];
-                        sum_sq += v[i] * v[i];
-                    }
-                }
-            }
-    float sum_dot = 0.f;
-    for (int i = 0; i < 3; i++) sum_dot += sum[i] * sum[i];
-    p->density_variation_scaling_factor = -1.f / (beta * (-sum_dot - sum_sq));
-}
-
-struct DeviceGuard {
-    int prev = -1;
-    explicit DeviceGuard(int dev) {
-        cudaGetDevice(&prev);
-        if (prev != dev) cudaSetDevice(dev);
-    }
-    ~DeviceGuard() {
-        int cur = -1;
-        cudaGetDevice(&cur);
-        if (prev >= 0 && cur != prev) cudaSetDevice(prev);
-    }
-};
-
-struct DeviceBlock {
-    void* p = nullptr;
-    size_t cap = 0;
-    cudaError_t ensure(size_t bytes) {
-        if (bytes <= cap && p) return cudaSuccess;
-        if (p) cudaFree(p);
-        p = nullptr;
-        cap = 0;
-        cudaError_t e = cudaMalloc(&p, std::max<size_t>(bytes, 256));
-        if (e == cudaSuccess) cap = std::max<size_t>(bytes, 256);
-        return e;
-    }
-    void release() {
-        if (p) cudaFree(p);
-        p = nullptr;
-        cap = 0;
-    }
-};
-
-struct Carver {
-    unsigned char* base;
-    size_t off = 0;
-    template <class T>
-    T* take(size_t count) {
-        T* r = reinterpret_cast<T*>(base + off);
-        off += align256(count * sizeof(T));
-        return r;
-    }
-};
 
 size_t fluid_arena_bytes(uint32_t n, uint32_t bk) {
     return 10 * align256((size_t)n * 16) + 3 * align256((size_t)n * 4) + 4 * align256((size_t)n * 4) +
@@ -186,22 +84,23 @@ struct pcisph_ctx {
     RadixSorter sorter;
     DevParams P{};
     SweepGrid sweep_grid{};
-    uint32_t* morton = nullptr;   // Morton codes for the working order (list block)
-    uint32_t* work_buf = nullptr;
-    RadixSorter work_sorter;      // sorts the Morton codes (allocates its scratch on first use)
     size_t list_n = 0;
-    static constexpr uint64_t kWorkOrderInterval = 16;
 
     SweepArgs sweep_args() const {
         return SweepArgs{b.groups, &b.ctl->n_groups, sorted_keys, b.cells, b.b_cells, b.codes, b.b_codes};
     }
     bool warp_sweeps() const { return opts.kernel_variant == 0; }
     bool list_sweeps() const { return opts.kernel_variant == 2; }
+    ListBuffers list_buffers() const {
+        return ListBuffers{b.pos, b.vel, b.pr4, b.normal, b.f_other, b.f_press, b.pred, b.pf4, b.state_pos,
+                           b.state_vel, b.rho, b.press, b.err, b.cells, b.b_cells, b.b_pos, b.bpf, b.nbr,
+                           b.nbr_count, b.bucket_fast};
+    }
 
     int ensure_lists() {
         if (!list_sweeps()) return PCISPH_OK;
         const size_t n = params.fluid_count;
-        const size_t bytes = align256(n * P.list_cap * 4) + 3 * align256(n * 4) + align256(params.bucket_count);
+        const size_t bytes = align256(n * P.list_cap * 4) + align256(n * 4) + align256(params.bucket_count);
         if (list_block.p && list_block.cap >= bytes && list_n == n) return PCISPH_OK;
         CUDA_TRY(cudaStreamSynchronize(stream()));
         if (list_block.ensure(bytes) != cudaSuccess)
@@ -209,31 +108,12 @@ struct pcisph_ctx {
         Carver c{static_cast<unsigned char*>(list_block.p)};
         b.nbr = c.take<uint32_t>(n * P.list_cap);
         b.nbr_count = c.take<uint32_t>(n);
-        work_buf = c.take<uint32_t>(n);
-        morton = c.take<uint32_t>(n);
         b.bucket_fast = c.take<unsigned char>(params.bucket_count);
-        b.work = nullptr;  // identity working order
-        CUDA_TRY(cudaGetLastError());
         list_n = n;
         graph_valid = false;
         return PCISPH_OK;
     }
 
-    // Working order of the list sweeps: this step's sorted particles ordered by the Morton code of their
-    // cell. Run after a step (stream-ordered), used by the next steps; refreshed every kWorkOrderInterval.
-    int refresh_work_order(cudaStream_t s) {
-        if (!list_sweeps() || !work_buf) return PCISPH_OK;
-        b.work = work_buf;
-        const uint32_t n = params.fluid_count;
-        launch_morton(b.pos, n, P, morton, s);
-        uint32_t *sk = nullptr, *sv = nullptr;
-        // a sorter of its own: the step's sorter scratch holds this step's sorted keys and ids
-        cudaError_t e = work_sorter.sort(morton, b.work, n, 30, true, s, &sk, &sv);
-        if (e != cudaSuccess) return fail(PCISPH_ERR_CUDA, std::string("work-order sort: ") + cudaGetErrorString(e));
-        if (sv != b.work) CUDA_TRY(cudaMemcpyAsync(b.work, sv, (size_t)n * 4, cudaMemcpyDeviceToDevice, s));
-        host_launches += 1 + work_sorter.last_launches();
-        return PCISPH_OK;
-    }
 
     cudaGraphExec_t graph_exec = nullptr;
     bool graph_valid = false;
@@ -327,41 +207,8 @@ struct pcisph_ctx {
 
     // -------------------------------------------------------- parameters
     void build_devparams() {
-        DevParams& d = P;
-        d.particle_mass = params.particle_mass;
-        d.rest_density = params.rest_density;
-        d.h = params.kernel_radius;
-        d.h2 = params.kernel_radius2;
-        d.cell_size = params.cell_size;
-        d.poly6_norm = params.poly6_normalization;
-        d.poly6_d1_norm = params.poly6_d1_normalization;
-        d.visc_d2_norm = params.viscosity_d2_normalization;
-        d.spiky_d1_norm = params.spiky_d1_normalization;
-        d.st_coeff = params.surface_tension_coefficient;
-        d.st_term = params.surface_tension_term;
-        d.st_norm = params.surface_tension_normalization;
-        d.viscosity = params.viscosity_constant;
-        d.gravity = params.gravity;
-        d.dt = params.delta_t;
-        d.delta = params.density_variation_scaling_factor;
-        d.fluid_count = params.fluid_count;
-        d.boundary_count = params.boundary_count;
-        d.bucket_count = params.bucket_count;
-        magic_for(params.bucket_count, &d.bk_magic, &d.bk_shift);
-        d.min_iters = opts.min_iterations;
-        d.max_iters = opts.max_iterations;
-        d.walls = opts.walls;
-        for (int a = 0; a < 3; a++) {
-            d.box_lo[a] = opts.box_lo[a];
-            d.box_hi[a] = opts.box_hi[a];
-        }
-        d.restitution = opts.restitution;
-        d.threshold = threshold;
-        d.list_cap = kListCap;
-        d.list_r = params.kernel_radius * (1.f + opts.list_skin);
-        d.list_r2 = d.list_r * d.list_r;
-        // half the skin, less a margin for the rounding of |x_i - x_j| and |x* - x| (relative 1e-6 of h)
-        d.list_half_skin = 0.5f * params.kernel_radius * opts.list_skin - 1e-6f * params.kernel_radius;
+        make_devparams(params, opts.min_iterations, opts.max_iterations, opts.walls, opts.box_lo, opts.box_hi,
+                       opts.restitution, threshold, opts.list_skin, 0, &P);
         graph_valid = false;
     }
 
@@ -472,8 +319,8 @@ struct pcisph_ctx {
         timed("reorder", s, [&] { launch_reorder(sk, sv, b.state_pos, b.state_vel, N, b.pos, b.vel, b.cells, b.codes, b.groups, P, b.ctl, s); });
         const SweepArgs A = sweep_args();
         if (list_sweeps()) {
-            timed("density", s, [&] { launch_density_list(P, b, s); });
-            timed("normal", s, [&] { launch_normal_list(P, b, s); });
+            timed("density", s, [&] { launch_density_list(P, b.ctl, list_buffers(), s); });
+            timed("normal", s, [&] { launch_normal_list(P, b.ctl, list_buffers(), s); });
         } else if (warp_sweeps()) {
             timed("density", s, [&] { launch_density_sweep(P, b, A, sweep_grid, s); });
             timed("normal", s, [&] { launch_normal_sweep(P, b, A, sweep_grid, s); });
@@ -482,7 +329,7 @@ struct pcisph_ctx {
             timed("normal", s, [&] { launch_normal(P, b, s); });
         }
         if (B && cudaMemsetAsync(b.b_press, 0, (size_t)B * 4, s) != cudaSuccess) return -1;
-        if (list_sweeps()) timed("force", s, [&] { launch_force_list(P, b, s); });
+        if (list_sweeps()) timed("force", s, [&] { launch_force_list(P, b.ctl, list_buffers(), s); });
         else if (warp_sweeps()) timed("force", s, [&] { launch_force_sweep(P, b, A, sweep_grid, s); });
         else timed("force", s, [&] { launch_force(P, b, s); });
         nl += 4;
@@ -497,8 +344,8 @@ struct pcisph_ctx {
             ++nl;
         }
         if (list_sweeps()) {
-            timed("pressure", s, [&] { launch_pressure_list(P, b, s); });
-            timed("pressure_force", s, [&] { launch_pressure_force_list(P, b, 0, cond, use_cond, s); });
+            timed("pressure", s, [&] { launch_pressure_list(P, b.ctl, list_buffers(), s); });
+            timed("pressure_force", s, [&] { launch_pressure_force_list(P, b.ctl, list_buffers(), 0, cond, use_cond, s); });
         } else if (warp_sweeps()) {
             const SweepArgs A = sweep_args();
             timed("pressure", s, [&] { launch_pressure_sweep(P, b, A, sweep_grid, s); });
@@ -648,32 +495,32 @@ struct pcisph_ctx {
                 break;
             }
             case PCISPH_STAGE_DENSITY:
-                if (list_sweeps()) launch_density_list(P, b, s);
+                if (list_sweeps()) launch_density_list(P, b.ctl, list_buffers(), s);
                 else if (warp_sweeps()) launch_density_sweep(P, b, sweep_args(), sweep_grid, s);
                 else launch_density(P, b, s);
                 ++host_launches;
                 break;
             case PCISPH_STAGE_NORMAL:
-                if (list_sweeps()) launch_normal_list(P, b, s);
+                if (list_sweeps()) launch_normal_list(P, b.ctl, list_buffers(), s);
                 else if (warp_sweeps()) launch_normal_sweep(P, b, sweep_args(), sweep_grid, s);
                 else launch_normal(P, b, s);
                 ++host_launches;
                 break;
             case PCISPH_STAGE_FORCE:
-                if (list_sweeps()) launch_force_list(P, b, s);
+                if (list_sweeps()) launch_force_list(P, b.ctl, list_buffers(), s);
                 else if (warp_sweeps()) launch_force_sweep(P, b, sweep_args(), sweep_grid, s);
                 else launch_force(P, b, s);
                 ++host_launches;
                 break;
             case PCISPH_STAGE_BOUNDARY_PRESSURE: launch_boundary_pressure(P, b, s); ++host_launches; break;
             case PCISPH_STAGE_PRESSURE:
-                if (list_sweeps()) launch_pressure_list(P, b, s);
+                if (list_sweeps()) launch_pressure_list(P, b.ctl, list_buffers(), s);
                 else if (warp_sweeps()) launch_pressure_sweep(P, b, sweep_args(), sweep_grid, s);
                 else launch_pressure(P, b, s);
                 ++host_launches;
                 break;
             case PCISPH_STAGE_PRESSURE_FORCE:
-                if (list_sweeps()) launch_pressure_force_list(P, b, arg ? 2 : 1, 0, false, s);
+                if (list_sweeps()) launch_pressure_force_list(P, b.ctl, list_buffers(), arg ? 2 : 1, 0, false, s);
                 else if (warp_sweeps()) launch_pressure_force_sweep(P, b, sweep_args(), sweep_grid, arg ? 2 : 1, 0, false, s);
                 else launch_pressure_force(P, b, arg ? 2 : 1, 0, false, s);
                 ++host_launches;

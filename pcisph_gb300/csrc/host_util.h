@@ -1,0 +1,167 @@
+// host_util.h -- host-side helpers shared by the step context (context.cu) and the batch (batch.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <string>
+
+#include "../../include/pcisph_gpu.h"
+#include "common.cuh"
+
+namespace pcisph {
+
+int report_error(int code, const std::string& msg);  // context.cu: sets pcisph_last_error()
+
+namespace host {
+
+inline size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
+
+inline constexpr float kPi = 3.14159265358979323846f;  // utils/constants.h:4
+inline constexpr uint32_t kListCap = 96;           // neighbour-list entries per particle (multiple of 4)
+
+// Fluid.cpp:125-133
+inline uint32_t sort_bit_count_ref(uint32_t elements) {
+    uint32_t max_value = 0;
+    for (int i = 0; i < 32; i++) {
+        max_value = (max_value << 1) | 1u;
+        if (max_value >= elements - 1u) return (uint32_t)(i + 1);
+    }
+    return 32u;
+}
+
+// Bits needed for keys < bucket_count.
+inline int key_bits(uint32_t bucket_count) {
+    int b = 1;
+    while (b < 32 && (1ull << b) < (unsigned long long)bucket_count) ++b;
+    return b;
+}
+
+// update_deduced_attributes (Fluid.cpp:377-443): the same expressions, so the same floats.
+inline void derive(pcisph_sim_params* p) {
+    p->kernel_radius = 4.f * p->particle_radius;
+    p->kernel_radius2 = std::pow(p->kernel_radius, 2.f);
+    p->particle_mass = (float)((double)p->rest_density / std::pow((double)(1.f / (2.f * p->particle_radius)), 3.0));
+    p->bucket_count = p->fluid_count / 2;
+    p->bucket_count -= p->bucket_count % 64;
+    p->bucket_count = std::max(64u, p->bucket_count);
+    p->cell_size = p->kernel_radius;
+    p->poly6_normalization = 315.f / (64.f * kPi * std::pow(p->kernel_radius, 9.f));
+    p->poly6_d1_normalization = -945.f / (32.f * kPi * std::pow(p->kernel_radius, 9.f));
+    p->viscosity_d2_normalization = 45.f / (kPi * std::pow(p->kernel_radius, 6.0f));
+    p->spiky_d1_normalization = -45.f / (kPi * std::pow(p->kernel_radius, 6.0f));
+    p->surface_tension_normalization = 32.f / (kPi * std::pow(p->kernel_radius, 9.f));
+    p->surface_tension_term = std::pow(p->kernel_radius, 6.f) / 64.f;
+    const float particle_size = 2.f * p->particle_radius;
+    const float beta = p->delta_t * p->delta_t * p->particle_mass * p->particle_mass * 2.f /
+                       (p->rest_density * p->rest_density);
+    float sum[3] = {0.f, 0.f, 0.f}, sum_sq = 0.f;
+    const float lim = p->kernel_radius + particle_size;
+    for (float z = -p->kernel_radius - particle_size; z <= lim; z += 2.f * p->particle_radius)
+        for (float y = -p->kernel_radius - particle_size; y <= lim; y += 2.f * p->particle_radius)
+            for (float x = -p->kernel_radius - particle_size; x <= lim; x += 2.f * p->particle_radius) {
+                const float r = std::sqrt(x * x + y * y + z * z);
+                const float r2 = r * r;
+                if (r2 < p->kernel_radius2) {
+                    const float f = (float)((double)p->poly6_d1_normalization *
+                                            std::pow((double)(p->kernel_radius2 - r2), 2.0));
+                    const float v[3] = {-f * x, -f * y, -f * z};
+                    for (int i = 0; i < 3; i++) {
+                        sum[i] += v[i];
+                        sum_sq += v[i] * v[i];
+                    }
+                }
+            }
+    float sum_dot = 0.f;
+    for (int i = 0; i < 3; i++) sum_dot += sum[i] * sum[i];
+    p->density_variation_scaling_factor = -1.f / (beta * (-sum_dot - sum_sq));
+}
+
+struct DeviceGuard {
+    int prev = -1;
+    explicit DeviceGuard(int dev) {
+        cudaGetDevice(&prev);
+        if (prev != dev) cudaSetDevice(dev);
+    }
+    ~DeviceGuard() {
+        int cur = -1;
+        cudaGetDevice(&cur);
+        if (prev >= 0 && cur != prev) cudaSetDevice(prev);
+    }
+};
+
+struct DeviceBlock {
+    void* p = nullptr;
+    size_t cap = 0;
+    cudaError_t ensure(size_t bytes) {
+        if (bytes <= cap && p) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+        cudaError_t e = cudaMalloc(&p, std::max<size_t>(bytes, 256));
+        if (e == cudaSuccess) cap = std::max<size_t>(bytes, 256);
+        return e;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+    }
+};
+
+struct Carver {
+    unsigned char* base;
+    size_t off = 0;
+    template <class T>
+    T* take(size_t count) {
+        T* r = reinterpret_cast<T*>(base + off);
+        off += align256(count * sizeof(T));
+        return r;
+    }
+};
+
+// Kernel parameters of one scene from its reference parameters and step options.
+inline void make_devparams(const pcisph_sim_params& p, int min_iters, int max_iters, int walls, const float* box_lo,
+                           const float* box_hi, float restitution, float threshold, float list_skin,
+                           uint32_t bucket_base, DevParams* d) {
+    *d = DevParams{};
+    d->particle_mass = p.particle_mass;
+    d->rest_density = p.rest_density;
+    d->h = p.kernel_radius;
+    d->h2 = p.kernel_radius2;
+    d->cell_size = p.cell_size;
+    d->poly6_norm = p.poly6_normalization;
+    d->poly6_d1_norm = p.poly6_d1_normalization;
+    d->visc_d2_norm = p.viscosity_d2_normalization;
+    d->spiky_d1_norm = p.spiky_d1_normalization;
+    d->st_coeff = p.surface_tension_coefficient;
+    d->st_term = p.surface_tension_term;
+    d->st_norm = p.surface_tension_normalization;
+    d->viscosity = p.viscosity_constant;
+    d->gravity = p.gravity;
+    d->dt = p.delta_t;
+    d->delta = p.density_variation_scaling_factor;
+    d->fluid_count = p.fluid_count;
+    d->boundary_count = p.boundary_count;
+    d->bucket_count = p.bucket_count;
+    magic_for(p.bucket_count, &d->bk_magic, &d->bk_shift);
+    d->bucket_base = bucket_base;
+    d->list_cap = kListCap;
+    d->list_r = p.kernel_radius * (1.f + list_skin);
+    d->list_r2 = d->list_r * d->list_r;
+    // half the skin, less a margin for the rounding of |x_i - x_j| and |x* - x| (relative 1e-6 of h)
+    d->list_half_skin = 0.5f * p.kernel_radius * list_skin - 1e-6f * p.kernel_radius;
+    d->min_iters = min_iters;
+    d->max_iters = max_iters;
+    d->walls = walls;
+    for (int a = 0; a < 3; a++) {
+        d->box_lo[a] = box_lo[a];
+        d->box_hi[a] = box_hi[a];
+    }
+    d->restitution = restitution;
+    d->threshold = threshold;
+}
+
+}  // namespace host
+}  // namespace pcisph

@@ -1,4 +1,4 @@
-// list_kernels.cu -- neighbour-list sweeps (kernel_variant 2).
+// list_kernels.cu -- neighbour-list sweeps (kernel_variant 2), for one scene or a batch of scenes.
 //
 // The density sweep walks the reference's 27 buckets (grid_utils.cl:65-79) once per step and records,
 // per particle, every candidate j with |x_i - x_j| <= r_list = h (1 + skin), in walk order. The later
@@ -18,15 +18,15 @@
 //     fast particle j in i's walk (spatial neighbour or hash collision) is then summed by a walk. Flags
 //     last for the rest of the step;
 //   - a particle with more than list_cap candidates is marked (count > cap) and walks the buckets.
-// Boundary particles (B > 0) are summed by walking the boundary buckets, as in the other variants.
+// Boundary particles (B > 0, single scene) are summed by walking the boundary buckets.
 //
-// All arrays stay in the reference's sorted order (hash order, which scatters neighbouring cells across
-// memory). Threads are mapped to particles through a "working order" instead: a permutation sorted by the
-// Morton code of each particle's cell, so that the 32 particles of a warp are spatial neighbours and their
-// neighbour gathers hit the same cache lines. Any permutation gives the same results (each particle's
-// sum is independent of which thread computes it); the working order is only refreshed every few steps.
+// Parameter sources (list_kernels.cuh): OneScene passes one DevParams by value and the pressure kernel's
+// last block decides the loop. SceneTable serves a batch: particle i belongs to scene scene_of[i], whose
+// DevParams (own particle count, bucket count and base in the shared cell table, box, limits) and Control
+// live in device tables. Scenes stay contiguous in the sorted arrays because each scene's keys occupy its
+// own bucket range. k_batch_decide closes each iteration per scene; finished scenes skip the sweeps.
+#include "list_kernels.cuh"
 #include "pair_terms.cuh"
-#include "step_kernels.cuh"
 
 namespace pcisph {
 namespace {
@@ -34,32 +34,15 @@ namespace {
 constexpr int kBlock = 256;
 inline unsigned grid_for(uint32_t n) { return (n + kBlock - 1) / kBlock; }
 
-// Particle handled by this thread (nullptr work: identity).
-__device__ __forceinline__ uint32_t particle_of(const uint32_t* __restrict__ work, uint32_t t) {
-    return work ? __ldg(&work[t]) : t;
+// atomicMax aggregated over the lanes of a warp that target the same address (one atomic per address).
+__device__ __forceinline__ void warp_atomic_max(unsigned* addr, unsigned v) {
+    const unsigned act = __activemask();
+    const unsigned peers = __match_any_sync(act, (unsigned long long)addr);
+    const unsigned m = __reduce_max_sync(peers, v);
+    if ((int)(threadIdx.x & 31) == __ffs(peers) - 1) atomicMax(addr, m);
 }
 
-// Spread the low 10 bits of v to every third bit (Morton interleave).
-__device__ __forceinline__ uint32_t spread3(uint32_t v) {
-    v &= 1023u;
-    v = (v | (v << 16)) & 0x030000FFu;
-    v = (v | (v << 8)) & 0x0300F00Fu;
-    v = (v | (v << 4)) & 0x030C30C3u;
-    v = (v | (v << 2)) & 0x09249249u;
-    return v;
-}
-
-// Morton code of each particle's cell (low 10 bits per axis; locality only) and the identity values.
-__global__ void __launch_bounds__(kBlock) k_morton(const float4* __restrict__ pos, uint32_t n, DevParams P,
-                                                   uint32_t* __restrict__ code) {
-    const uint32_t t = blockIdx.x * kBlock + threadIdx.x;
-    if (t >= n) return;
-    const float4 x = pos[t];
-    const Cell c = cell_of(x.x, x.y, x.z, P);
-    code[t] = spread3(c.x) | (spread3(c.y) << 1) | (spread3(c.z) << 2);
-}
-
-// Call f(j) for every listed neighbour, four indices per 16-byte load (independent gathers in flight).
+// Call f(j) for every listed neighbour, eight indices per two 16-byte loads (independent gathers in flight).
 template <class F>
 __device__ __forceinline__ void for_each_listed(const uint32_t* __restrict__ row, uint32_t n, F&& f) {
     const uint4* r4 = reinterpret_cast<const uint4*>(row);
@@ -80,24 +63,23 @@ __device__ __forceinline__ void for_each_listed(const uint32_t* __restrict__ row
     for (; k < n; ++k) f(__ldg(&row[k]));
 }
 
-// After predicting x*_i (stored as xs): record the step's max displacement; a fast particle flags its bucket.
+// After predicting x*_i (stored as xs): record the max displacement; a fast particle flags its bucket.
 __device__ __forceinline__ void note_displacement(const DevParams& P, Control* ctl,
                                                   unsigned char* __restrict__ bucket_fast, const float4& xi,
                                                   const float4& xs) {
     const float dx = xs.x - xi.x, dy = xs.y - xi.y, dz = xs.z - xi.z;  // exact: xs and xi are close
     const float disp = sqrtf(dx * dx + dy * dy + dz * dz);
-    const unsigned act = __activemask();
-    const unsigned m = __reduce_max_sync(act, __float_as_uint(disp));
-    if ((int)(threadIdx.x & 31) == __ffs(act) - 1) atomicMax(&ctl->max_disp_bits, m);
+    warp_atomic_max(&ctl->max_disp_bits, __float_as_uint(disp));
     if (disp > P.list_half_skin) {
         atomicAdd(&ctl->fast_particles, 1ull);
         const Cell c = cell_of(xi.x, xi.y, xi.z, P);
-        bucket_fast[hash_key(c.x, c.y, c.z, P)] = 1;
+        bucket_fast[P.bucket_base + hash_key(c.x, c.y, c.z, P)] = 1;
     }
 }
 
 // Does any of the 27 buckets around c hold a fast particle this step?
-__device__ __forceinline__ bool near_fast(const DevParams& P, const unsigned char* __restrict__ bucket_fast, const Cell& c) {
+__device__ __forceinline__ bool near_fast(const DevParams& P, const unsigned char* __restrict__ bucket_fast,
+                                          const Cell& c) {
     bool any = false;
 #pragma unroll 1
     for (int dz = -1; dz <= 1; ++dz) {
@@ -111,33 +93,50 @@ __device__ __forceinline__ bool near_fast(const DevParams& P, const unsigned cha
             for (int dx = -1; dx <= 1; ++dx) {
                 const uint32_t x = c.x + (uint32_t)dx;
                 const uint32_t v = (((x * 19349663u) ^ hyz) << 6) + (x & 63u) + lyz;
-                any |= bucket_fast[mod_bk(v & 0x7FFFFFFFu, P)] != 0;
+                any |= bucket_fast[P.bucket_base + mod_bk(v & 0x7FFFFFFFu, P)] != 0;
             }
         }
     }
     return any;
 }
 
+// The loop decision of one scene after its pressure sweep (Fluid.cpp:284-306).
+__device__ __forceinline__ void decide(const DevParams& P, Control* ctl) {
+    const float mx = __uint_as_float(ctl->max_err_bits);
+    const unsigned it = ctl->iter + 1;
+    const float rel = mx / P.rest_density;
+    const bool converged = rel < P.threshold;
+    const bool done = it >= (unsigned)P.max_iters || (it >= (unsigned)P.min_iters && converged);
+    ctl->iter = it;
+    ctl->done = done ? 1u : 0u;
+    ctl->max_err_bits = 0;
+    ctl->blocks_done = 0;
+    if (__uint_as_float(ctl->max_disp_bits) > P.list_half_skin) ctl->list_fallbacks += 1;
+    if (done) {
+        if (!converged) ctl->status |= 1u;
+        ctl->status_all |= ctl->status;
+        ctl->iterations_last = (int)it;
+        ctl->max_err_last = rel;
+        ctl->steps += 1;
+        ctl->total_iters += it;
+    }
+}
+
 // pcisph.cl:65-92, and the neighbour list of the step
-__global__ void __launch_bounds__(kBlock) k_density_list(DevParams P, const uint2* __restrict__ b_cells,
-                                                         const float4* __restrict__ b_pos,
-                                                         const uint2* __restrict__ cells,
-                                                         const float4* __restrict__ pos, float* __restrict__ rho,
-                                                         float4* __restrict__ pr4, uint32_t* __restrict__ nbr,
-                                                         uint32_t* __restrict__ nbr_count,
-                                                         const uint32_t* __restrict__ work) {
-    const uint32_t t = blockIdx.x * kBlock + threadIdx.x;
-    if (t >= P.fluid_count) return;
-    const uint32_t i = particle_of(work, t);
-    const float4 xi = pos[i];
+template <class PS>
+__global__ void __launch_bounds__(kBlock) k_density_list(PS ps, ListBuffers b) {
+    const uint32_t i = blockIdx.x * kBlock + threadIdx.x;
+    if (i >= ps.count()) return;
+    const DevParams& P = ps.params(i);
+    const float4 xi = b.pos[i];
     const Cell c = cell_of(xi.x, xi.y, xi.z, P);
     float acc = 0.f;
     if (P.boundary_count)
-        for_each_neighbour(b_cells, c, P, [&](uint32_t j) { acc += density_term(xi.x, xi.y, xi.z, __ldg(&b_pos[j]), P.h2); });
-    uint32_t* row = nbr + (size_t)i * P.list_cap;
+        for_each_neighbour(b.b_cells, c, P, [&](uint32_t j) { acc += density_term(xi.x, xi.y, xi.z, __ldg(&b.b_pos[j]), P.h2); });
+    uint32_t* row = b.nbr + (size_t)i * P.list_cap;
     uint32_t n = 0;
-    for_each_neighbour(cells, c, P, [&](uint32_t j) {
-        const float4 o = __ldg(&pos[j]);
+    for_each_neighbour(b.cells, c, P, [&](uint32_t j) {
+        const float4 o = __ldg(&b.pos[j]);
         const float dx = xi.x - o.x, dy = xi.y - o.y, dz = xi.z - o.z;
         const float r2 = dx * dx + dy * dy + dz * dz;
         acc += poly6(r2, P.h2);
@@ -146,112 +145,101 @@ __global__ void __launch_bounds__(kBlock) k_density_list(DevParams P, const uint
             ++n;
         }
     });
-    nbr_count[i] = n;  // n > list_cap: this particle walks the buckets in the later sweeps
+    b.nbr_count[i] = n;  // n > list_cap: this particle walks the buckets in the later sweeps
     acc *= P.particle_mass * P.poly6_norm;
-    rho[i] = acc;
-    pr4[i] = make_float4(xi.x, xi.y, xi.z, acc);
+    b.rho[i] = acc;
+    b.pr4[i] = make_float4(xi.x, xi.y, xi.z, acc);
 }
 
 // pcisph.cl:94-112
-__global__ void __launch_bounds__(kBlock) k_normal_list(DevParams P, const uint2* __restrict__ cells,
-                                                        const float4* __restrict__ pr4, float4* __restrict__ normal,
-                                                        const uint32_t* __restrict__ nbr,
-                                                        const uint32_t* __restrict__ nbr_count,
-                                                        const uint32_t* __restrict__ work) {
-    const uint32_t t = blockIdx.x * kBlock + threadIdx.x;
-    if (t >= P.fluid_count) return;
-    const uint32_t i = particle_of(work, t);
-    const float4 xi = pr4[i];
+template <class PS>
+__global__ void __launch_bounds__(kBlock) k_normal_list(PS ps, ListBuffers b) {
+    const uint32_t i = blockIdx.x * kBlock + threadIdx.x;
+    if (i >= ps.count()) return;
+    const DevParams& P = ps.params(i);
+    const float4 xi = b.pr4[i];
     float3 n = make_float3(0.f, 0.f, 0.f);
-    const uint32_t cnt = nbr_count[i];
-    auto f = [&](uint32_t j) { normal_term(xi.x, xi.y, xi.z, __ldg(&pr4[j]), P.h2, n); };
-    if (cnt <= P.list_cap) for_each_listed(nbr + (size_t)i * P.list_cap, cnt, f);
-    else for_each_neighbour(cells, cell_of(xi.x, xi.y, xi.z, P), P, f);
+    const uint32_t cnt = b.nbr_count[i];
+    auto f = [&](uint32_t j) { normal_term(xi.x, xi.y, xi.z, __ldg(&b.pr4[j]), P.h2, n); };
+    if (cnt <= P.list_cap) for_each_listed(b.nbr + (size_t)i * P.list_cap, cnt, f);
+    else for_each_neighbour(b.cells, cell_of(xi.x, xi.y, xi.z, P), P, f);
     const float scale = P.h * P.particle_mass * P.poly6_d1_norm;
-    normal[i] = make_float4(n.x * scale, n.y * scale, n.z * scale, 0.f);
+    b.normal[i] = make_float4(n.x * scale, n.y * scale, n.z * scale, 0.f);
 }
 
 // pcisph.cl:121-173, then the first predict (pcisph.cl:175-193, F_p = 0)
-__global__ void __launch_bounds__(kBlock) k_force_list(DevParams P, const uint2* __restrict__ cells,
-                                                       const float4* __restrict__ pr4, const float4* __restrict__ vel,
-                                                       const float4* __restrict__ normal,
-                                                       float4* __restrict__ f_other, float* __restrict__ press,
-                                                       float4* __restrict__ pred, const uint32_t* __restrict__ nbr,
-                                                       const uint32_t* __restrict__ nbr_count, Control* ctl,
-                                                       const uint32_t* __restrict__ work,
-                                                       unsigned char* __restrict__ bucket_fast) {
-    const uint32_t t = blockIdx.x * kBlock + threadIdx.x;
-    if (t >= P.fluid_count) return;
-    const uint32_t i = particle_of(work, t);
-    const float4 xi = pr4[i];
-    const float3 vi = f3(vel[i]);
-    const float3 ni = f3(normal[i]);
+template <class PS>
+__global__ void __launch_bounds__(kBlock) k_force_list(PS ps, ListBuffers b) {
+    const uint32_t i = blockIdx.x * kBlock + threadIdx.x;
+    if (i >= ps.count()) return;
+    const DevParams& P = ps.params(i);
+    const float4 xi = b.pr4[i];
+    const float3 vi = f3(b.vel[i]);
+    const float3 ni = f3(b.normal[i]);
     ForceAccum fa{make_float3(0.f, 0.f, 0.f), make_float3(0.f, 0.f, 0.f), make_float3(0.f, 0.f, 0.f)};
-    const uint32_t cnt = nbr_count[i];
-    auto f = [&](uint32_t j) { force_term(xi, vi, ni, __ldg(&pr4[j]), f3(__ldg(&vel[j])), f3(__ldg(&normal[j])), P, fa); };
-    if (cnt <= P.list_cap) for_each_listed(nbr + (size_t)i * P.list_cap, cnt, f);
-    else for_each_neighbour(cells, cell_of(xi.x, xi.y, xi.z, P), P, f);
+    const uint32_t cnt = b.nbr_count[i];
+    auto f = [&](uint32_t j) {
+        force_term(xi, vi, ni, __ldg(&b.pr4[j]), f3(__ldg(&b.vel[j])), f3(__ldg(&b.normal[j])), P, fa);
+    };
+    if (cnt <= P.list_cap) for_each_listed(b.nbr + (size_t)i * P.list_cap, cnt, f);
+    else for_each_neighbour(b.cells, cell_of(xi.x, xi.y, xi.z, P), P, f);
     const float m = P.particle_mass;
     const float3 visc = fa.visc * (P.viscosity * m * P.visc_d2_norm);
     const float3 coh = fa.coh * (-P.st_coeff * m * m * P.st_norm);
     const float3 curv = fa.curv * (-P.st_coeff * m);
     const float3 fo = make_float3(0.f, m * P.gravity, 0.f) + visc + (coh + curv);
-    f_other[i] = f4(fo, 0.f);
-    press[i] = 0.f;
+    b.f_other[i] = f4(fo, 0.f);
+    b.press[i] = 0.f;
     const float3 v = vi + (fo / m) * P.dt;
     const float3 dx = v * P.dt;
     const float4 xs = make_float4(xi.x + dx.x, xi.y + dx.y, xi.z + dx.z, 0.f);
-    pred[i] = xs;
-    note_displacement(P, ctl, bucket_fast, xi, xs);
+    b.pred[i] = xs;
+    note_displacement(P, ps.control(i), b.bucket_fast, xi, xs);
 }
 
-// pcisph.cl:212-263 (boundary_update = 0) + the stop decision (Fluid.cpp:284-306)
-__global__ void __launch_bounds__(kBlock) k_pressure_list(DevParams P, const uint2* __restrict__ b_cells,
-                                                          const float4* __restrict__ b_pos,
-                                                          const uint2* __restrict__ cells,
-                                                          const float4* __restrict__ pos,
-                                                          const float4* __restrict__ pred,
-                                                          const float* __restrict__ rho, float* __restrict__ press,
-                                                          float* __restrict__ err, float4* __restrict__ pf4,
-                                                          const uint32_t* __restrict__ nbr,
-                                                          const uint32_t* __restrict__ nbr_count, Control* ctl,
-                                                          const uint32_t* __restrict__ work,
-                                                          const unsigned char* __restrict__ bucket_fast) {
-    const uint32_t t = blockIdx.x * kBlock + threadIdx.x;
-    // no particle moved more than half the skin: every list is complete for x* (no marks were made)
-    const bool all_lists_ok = __uint_as_float(*(volatile unsigned*)&ctl->max_disp_bits) <= P.list_half_skin;
+// pcisph.cl:212-263 (boundary_update = 0); one scene: also the stop decision in the last block
+template <class PS>
+__global__ void __launch_bounds__(kBlock) k_pressure_list(PS ps, ListBuffers b) {
+    const uint32_t i = blockIdx.x * kBlock + threadIdx.x;
     float dv = 0.f;
-    if (t < P.fluid_count) {
-        const uint32_t i = particle_of(work, t);
-        const float4 xi = pos[i];
-        const float4 xp = pred[i];
+    if (i < ps.count() && !ps.skip_pressure(i)) {
+        const DevParams& P = ps.params(i);
+        Control* ctl = ps.control(i);
+        // no particle of the scene moved more than half the skin: its lists are complete for x*
+        const bool all_lists_ok = __uint_as_float(ctl->max_disp_bits) <= P.list_half_skin;
+        const float4 xi = b.pos[i];
+        const float4 xp = b.pred[i];
         float acc = 0.f;
-        const uint32_t cnt = nbr_count[i];
+        const uint32_t cnt = b.nbr_count[i];
         const Cell c = cell_of(xi.x, xi.y, xi.z, P);
-        const bool walk = cnt > P.list_cap || (!all_lists_ok && near_fast(P, bucket_fast, c));
+        const bool walk = cnt > P.list_cap || (!all_lists_ok && near_fast(P, b.bucket_fast, c));
         if (P.boundary_count)
-            for_each_neighbour(b_cells, c, P, [&](uint32_t j) { acc += density_term(xp.x, xp.y, xp.z, __ldg(&b_pos[j]), P.h2); });
-        auto f = [&](uint32_t j) { acc += density_term(xp.x, xp.y, xp.z, __ldg(&pred[j]), P.h2); };
-        if (walk) for_each_neighbour(cells, c, P, f);
-        else for_each_listed(nbr + (size_t)i * P.list_cap, cnt, f);
+            for_each_neighbour(b.b_cells, c, P, [&](uint32_t j) { acc += density_term(xp.x, xp.y, xp.z, __ldg(&b.b_pos[j]), P.h2); });
+        auto f = [&](uint32_t j) { acc += density_term(xp.x, xp.y, xp.z, __ldg(&b.pred[j]), P.h2); };
+        if (walk) for_each_neighbour(b.cells, c, P, f);
+        else for_each_listed(b.nbr + (size_t)i * P.list_cap, cnt, f);
         acc *= P.particle_mass * P.poly6_norm;
         if (!isfinite(acc)) atomicOr(&ctl->status, 2u);
         dv = acc - P.rest_density;
         dv = 0.f < dv ? dv : 0.f;
-        err[i] = dv;
-        float p = press[i];
+        b.err[i] = dv;
+        float p = b.press[i];
         if (dv != 0.f) {
             p += dv * P.delta;
-            press[i] = p;
+            b.press[i] = p;
         }
-        const float r = rho[i];
-        pf4[i] = make_float4(xi.x, xi.y, xi.z, p / (r * r));
+        const float r = b.rho[i];
+        b.pf4[i] = make_float4(xi.x, xi.y, xi.z, p / (r * r));
+        if (PS::kBatched) warp_atomic_max(&ctl->max_err_bits, __float_as_uint(dv));
     }
-    unsigned bits = __reduce_max_sync(0xffffffffu, __float_as_uint(dv));
+    if (PS::kBatched) return;
+    // one scene: block max of dv, the last block decides (dv >= 0: bit patterns order like values)
+    const unsigned bits = __reduce_max_sync(0xffffffffu, __float_as_uint(dv));
     __shared__ unsigned warp_max[kBlock / 32];
     __shared__ bool is_last;
     if ((threadIdx.x & 31) == 0) warp_max[threadIdx.x >> 5] = bits;
     __syncthreads();
+    Control* ctl = ps.control(0);
     if (threadIdx.x == 0) {
         unsigned m = 0;
 #pragma unroll
@@ -263,67 +251,49 @@ __global__ void __launch_bounds__(kBlock) k_pressure_list(DevParams P, const uin
     __syncthreads();
     if (is_last && threadIdx.x == 0) {
         __threadfence();
-        const float mx = __uint_as_float(atomicAdd(&ctl->max_err_bits, 0u));
-        const unsigned it = ctl->iter + 1;
-        const float rel = mx / P.rest_density;
-        const bool converged = rel < P.threshold;
-        const bool done = it >= (unsigned)P.max_iters || (it >= (unsigned)P.min_iters && converged);
-        ctl->iter = it;
-        ctl->done = done ? 1u : 0u;
-        ctl->max_err_bits = 0;
-        ctl->blocks_done = 0;
-        if (!all_lists_ok) ctl->list_fallbacks += 1;
-        if (done) {
-            if (!converged) ctl->status |= 1u;
-            ctl->status_all |= ctl->status;
-            ctl->iterations_last = (int)it;
-            ctl->max_err_last = rel;
-            ctl->steps += 1;
-            ctl->total_iters += it;
-        }
+        ctl->max_err_bits = atomicAdd(&ctl->max_err_bits, 0u);  // see every block's contribution
+        decide(ps.params(0), ctl);
     }
 }
 
 // pcisph.cl:265-300, then predict (pcisph.cl:175-193) or integrate with optional walls
-__global__ void __launch_bounds__(kBlock) k_pressure_force_list(
-    DevParams P, const uint2* __restrict__ b_cells, const float4* __restrict__ bpf, const uint2* __restrict__ cells,
-    const float4* __restrict__ pf4, const float4* __restrict__ vel, const float4* __restrict__ f_other,
-    float4* __restrict__ f_press, float4* __restrict__ pred, float4* __restrict__ state_pos,
-    float4* __restrict__ state_vel, const uint32_t* __restrict__ nbr, const uint32_t* __restrict__ nbr_count,
-    Control* ctl, int mode, cudaGraphConditionalHandle cond, int use_cond, const uint32_t* __restrict__ work,
-    unsigned char* __restrict__ bucket_fast) {
-    const uint32_t t = blockIdx.x * kBlock + threadIdx.x;
-    if (use_cond && t == 0) {
+template <class PS>
+__global__ void __launch_bounds__(kBlock) k_pressure_force_list(PS ps, ListBuffers b, int mode,
+                                                                cudaGraphConditionalHandle cond, int use_cond) {
+    const uint32_t i = blockIdx.x * kBlock + threadIdx.x;
+    if (!PS::kBatched && use_cond && i == 0) {
         // continue the graph's while loop unless the step is done; the counter bounds it on its own
+        Control* ctl = ps.control(0);
         const unsigned g = ++ctl->guard_iters;
-        const bool stop = ctl->done != 0u || g >= (unsigned)P.max_iters;
+        const bool stop = ctl->done != 0u || g >= (unsigned)ps.params(0).max_iters;
         cudaGraphSetConditional(cond, stop ? 0u : 1u);
     }
-    if (t >= P.fluid_count) return;
-    const uint32_t i = particle_of(work, t);
-    const float4 xi = pf4[i];
+    if (i >= ps.count() || ps.skip_force(i)) return;
+    const DevParams& P = ps.params(i);
+    Control* ctl = ps.control(i);
+    const float4 xi = b.pf4[i];
     float3 f = make_float3(0.f, 0.f, 0.f);
-    const uint32_t cnt = nbr_count[i];
+    const uint32_t cnt = b.nbr_count[i];
     Cell c{0u, 0u, 0u};
     if (cnt > P.list_cap || P.boundary_count) c = cell_of(xi.x, xi.y, xi.z, P);
     if (P.boundary_count)
-        for_each_neighbour(b_cells, c, P, [&](uint32_t j) { pressure_force_term(xi, __ldg(&bpf[j]), P.h, P.h2, f); });
-    auto body = [&](uint32_t j) { pressure_force_term(xi, __ldg(&pf4[j]), P.h, P.h2, f); };
-    if (cnt <= P.list_cap) for_each_listed(nbr + (size_t)i * P.list_cap, cnt, body);
-    else for_each_neighbour(cells, c, P, body);
+        for_each_neighbour(b.b_cells, c, P, [&](uint32_t j) { pressure_force_term(xi, __ldg(&b.bpf[j]), P.h, P.h2, f); });
+    auto body = [&](uint32_t j) { pressure_force_term(xi, __ldg(&b.pf4[j]), P.h, P.h2, f); };
+    if (cnt <= P.list_cap) for_each_listed(b.nbr + (size_t)i * P.list_cap, cnt, body);
+    else for_each_neighbour(b.cells, c, P, body);
     const float m = P.particle_mass;
     const float scale = -P.spiky_d1_norm * m * m;
     const float3 fp = make_float3(f.x * scale, f.y * scale, f.z * scale);
-    f_press[i] = f4(fp, 0.f);
+    b.f_press[i] = f4(fp, 0.f);
     const bool integrate = mode == 0 ? (ctl->done != 0u) : mode == 2;
-    const float3 a = (f3(f_other[i]) + fp) / m;
-    float3 v = f3(vel[i]) + a * P.dt;
+    const float3 a = (f3(b.f_other[i]) + fp) / m;
+    float3 v = f3(b.vel[i]) + a * P.dt;
     const float3 dx = v * P.dt;
     float3 x = make_float3(xi.x + dx.x, xi.y + dx.y, xi.z + dx.z);
     if (!integrate) {
         const float4 xs = f4(x, 0.f);
-        pred[i] = xs;
-        note_displacement(P, ctl, bucket_fast, xi, xs);
+        b.pred[i] = xs;
+        note_displacement(P, ctl, b.bucket_fast, xi, xs);
         return;
     }
     if (P.walls) {
@@ -340,47 +310,127 @@ __global__ void __launch_bounds__(kBlock) k_pressure_force_list(
             }
         }
     }
-    state_pos[i] = f4(x, 0.f);
-    state_vel[i] = f4(v, 0.f);
+    b.state_pos[i] = f4(x, 0.f);
+    b.state_vel[i] = f4(v, 0.f);
+}
+
+// Batch: close one corrective iteration per scene (one thread per scene) and set the graph's loop
+// condition: continue while some scene iterates. A scene decided done here is integrated by the
+// pressure-force sweep that follows; the next call marks it finished. Every scene is done by its
+// max_iters, so the loop ends; the guard bounds it by the largest max_iters on its own.
+__global__ void k_batch_decide(const DevParams* __restrict__ table, Control* ctls, uint32_t n_scenes, Control* batch,
+                               int max_iters, cudaGraphConditionalHandle cond, int use_cond) {
+    __shared__ int running;
+    if (threadIdx.x == 0) running = 0;
+    __syncthreads();
+    for (uint32_t s = threadIdx.x; s < n_scenes; s += blockDim.x) {
+        Control* c = &ctls[s];
+        if (c->done) {
+            c->finished = 1;
+            continue;
+        }
+        decide(table[s], c);
+        if (!c->done) atomicOr(&running, 1);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const unsigned g = ++batch->guard_iters;
+        batch->total_iters += 1;
+        const bool more = running != 0 && g < (unsigned)max_iters;
+        batch->any_running = more ? 1u : 0u;
+        if (use_cond) cudaGraphSetConditional(cond, more ? 1u : 0u);
+    }
+}
+
+// Batch step start: per-scene iteration state.
+__global__ void k_batch_begin(Control* ctls, uint32_t n_scenes, Control* batch) {
+    for (uint32_t s = threadIdx.x; s < n_scenes; s += blockDim.x) {
+        Control* c = &ctls[s];
+        c->iter = 0;
+        c->done = 0;
+        c->finished = 0;
+        c->max_err_bits = 0;
+        c->max_disp_bits = 0;
+        c->status = 0;
+    }
+    if (threadIdx.x == 0) {
+        batch->guard_iters = 0;
+        batch->any_running = 1;
+        batch->status = 0;  // the reorder flags an out-of-range sorted index here
+    }
+}
+
+__global__ void __launch_bounds__(kBlock) k_scene_of(const uint32_t* __restrict__ offsets, uint32_t n_scenes,
+                                                     uint32_t n, uint16_t* __restrict__ scene_of) {
+    const uint32_t i = blockIdx.x * kBlock + threadIdx.x;
+    if (i >= n) return;
+    uint32_t lo = 0, hi = n_scenes;  // largest s with offsets[s] <= i
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (offsets[mid] <= i) lo = mid;
+        else hi = mid;
+    }
+    scene_of[i] = (uint16_t)lo;
+}
+
+// sort_utils.cl:12-23 per scene, offset into the scene's bucket range of the shared table
+__global__ void __launch_bounds__(kBlock) k_hash_scenes(SceneTable ps, const float4* __restrict__ pos,
+                                                        uint32_t* __restrict__ keys) {
+    const uint32_t i = blockIdx.x * kBlock + threadIdx.x;
+    if (i >= ps.count()) return;
+    const DevParams& P = ps.params(i);
+    const float4 p = pos[i];
+    const Cell c = cell_of(p.x, p.y, p.z, P);
+    keys[i] = P.bucket_base + hash_key(c.x, c.y, c.z, P);
 }
 
 }  // namespace
 
-__global__ void __launch_bounds__(kBlock) k_iota(uint32_t* __restrict__ out, uint32_t n) {
-    const uint32_t t = blockIdx.x * kBlock + threadIdx.x;
-    if (t < n) out[t] = t;
+void launch_density_list(const DevParams& P, Control* ctl, const ListBuffers& b, cudaStream_t s) {
+    k_density_list<<<grid_for(P.fluid_count), kBlock, 0, s>>>(OneScene{P, ctl}, b);
+}
+void launch_normal_list(const DevParams& P, Control* ctl, const ListBuffers& b, cudaStream_t s) {
+    k_normal_list<<<grid_for(P.fluid_count), kBlock, 0, s>>>(OneScene{P, ctl}, b);
+}
+void launch_force_list(const DevParams& P, Control* ctl, const ListBuffers& b, cudaStream_t s) {
+    k_force_list<<<grid_for(P.fluid_count), kBlock, 0, s>>>(OneScene{P, ctl}, b);
+}
+void launch_pressure_list(const DevParams& P, Control* ctl, const ListBuffers& b, cudaStream_t s) {
+    k_pressure_list<<<grid_for(P.fluid_count), kBlock, 0, s>>>(OneScene{P, ctl}, b);
+}
+void launch_pressure_force_list(const DevParams& P, Control* ctl, const ListBuffers& b, int mode,
+                                cudaGraphConditionalHandle cond, bool use_cond, cudaStream_t s) {
+    k_pressure_force_list<<<grid_for(P.fluid_count), kBlock, 0, s>>>(OneScene{P, ctl}, b, mode, cond,
+                                                                      use_cond ? 1 : 0);
 }
 
-void launch_iota(uint32_t* out, uint32_t n, cudaStream_t s) {
-    if (n) k_iota<<<grid_for(n), kBlock, 0, s>>>(out, n);
+void launch_batch_begin(Control* ctls, uint32_t n_scenes, Control* batch, cudaStream_t s) {
+    k_batch_begin<<<1, 256, 0, s>>>(ctls, n_scenes, batch);
 }
-
-void launch_morton(const float4* pos, uint32_t n, const DevParams& P, uint32_t* code, cudaStream_t s) {
-    if (n) k_morton<<<grid_for(n), kBlock, 0, s>>>(pos, n, P, code);
+void launch_scene_of(const uint32_t* offsets, uint32_t n_scenes, uint32_t n, uint16_t* scene_of, cudaStream_t s) {
+    if (n) k_scene_of<<<grid_for(n), kBlock, 0, s>>>(offsets, n_scenes, n, scene_of);
 }
-
-void launch_density_list(const DevParams& P, const StepBuffers& b, cudaStream_t s) {
-    k_density_list<<<grid_for(P.fluid_count), kBlock, 0, s>>>(P, b.b_cells, b.b_pos, b.cells, b.pos, b.rho, b.pr4, b.nbr,
-                                                               b.nbr_count, b.work);
+void launch_hash_scenes(const SceneTable& t, const float4* pos, uint32_t* keys, cudaStream_t s) {
+    if (t.n) k_hash_scenes<<<grid_for(t.n), kBlock, 0, s>>>(t, pos, keys);
 }
-void launch_normal_list(const DevParams& P, const StepBuffers& b, cudaStream_t s) {
-    k_normal_list<<<grid_for(P.fluid_count), kBlock, 0, s>>>(P, b.cells, b.pr4, b.normal, b.nbr, b.nbr_count, b.work);
+void launch_density_scenes(const SceneTable& t, const ListBuffers& b, cudaStream_t s) {
+    if (t.n) k_density_list<<<grid_for(t.n), kBlock, 0, s>>>(t, b);
 }
-void launch_force_list(const DevParams& P, const StepBuffers& b, cudaStream_t s) {
-    k_force_list<<<grid_for(P.fluid_count), kBlock, 0, s>>>(P, b.cells, b.pr4, b.vel, b.normal, b.f_other, b.press, b.pred,
-                                                             b.nbr, b.nbr_count, b.ctl, b.work, b.bucket_fast);
+void launch_normal_scenes(const SceneTable& t, const ListBuffers& b, cudaStream_t s) {
+    if (t.n) k_normal_list<<<grid_for(t.n), kBlock, 0, s>>>(t, b);
 }
-void launch_pressure_list(const DevParams& P, const StepBuffers& b, cudaStream_t s) {
-    k_pressure_list<<<grid_for(P.fluid_count), kBlock, 0, s>>>(P, b.b_cells, b.b_pos, b.cells, b.pos, b.pred, b.rho,
-                                                                b.press, b.err, b.pf4, b.nbr, b.nbr_count, b.ctl, b.work,
-                                                                b.bucket_fast);
+void launch_force_scenes(const SceneTable& t, const ListBuffers& b, cudaStream_t s) {
+    if (t.n) k_force_list<<<grid_for(t.n), kBlock, 0, s>>>(t, b);
 }
-void launch_pressure_force_list(const DevParams& P, const StepBuffers& b, int mode, cudaGraphConditionalHandle cond,
-                                bool use_cond, cudaStream_t s) {
-    k_pressure_force_list<<<grid_for(P.fluid_count), kBlock, 0, s>>>(P, b.b_cells, b.bpf, b.cells, b.pf4, b.vel,
-                                                                      b.f_other, b.f_press, b.pred, b.state_pos,
-                                                                      b.state_vel, b.nbr, b.nbr_count, b.ctl, mode,
-                                                                      cond, use_cond ? 1 : 0, b.work, b.bucket_fast);
+void launch_pressure_scenes(const SceneTable& t, const ListBuffers& b, cudaStream_t s) {
+    if (t.n) k_pressure_list<<<grid_for(t.n), kBlock, 0, s>>>(t, b);
+}
+void launch_pressure_force_scenes(const SceneTable& t, const ListBuffers& b, cudaStream_t s) {
+    if (t.n) k_pressure_force_list<<<grid_for(t.n), kBlock, 0, s>>>(t, b, 0, 0, 0);
+}
+void launch_batch_decide(const SceneTable& t, Control* batch, int max_iters, cudaGraphConditionalHandle cond,
+                         bool use_cond, cudaStream_t s) {
+    k_batch_decide<<<1, 256, 0, s>>>(t.table, t.ctls, t.n_scenes, batch, max_iters, cond, use_cond ? 1 : 0);
 }
 
 }  // namespace pcisph

@@ -1,0 +1,71 @@
+// list_kernels.cuh -- neighbour-list sweeps for one scene or a batch of scenes (list_kernels.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+
+namespace pcisph {
+
+// Arrays the list sweeps read and write (sorted order; a batch concatenates its scenes).
+struct ListBuffers {
+    const float4 *pos, *vel;
+    float4 *pr4, *normal, *f_other, *f_press, *pred, *pf4, *state_pos, *state_vel;
+    float *rho, *press, *err;
+    const uint2* cells;
+    const uint2* b_cells;
+    const float4 *b_pos, *bpf;
+    uint32_t* nbr;               // list_cap entries per particle
+    uint32_t* nbr_count;         // entries per particle; > list_cap: walk the buckets
+    unsigned char* bucket_fast;  // per bucket of the cell table: holds a fast particle this step
+};
+
+// One scene: parameters by value; the pressure kernel's last block decides the loop.
+struct OneScene {
+    DevParams P;
+    Control* ctl;
+    static constexpr bool kBatched = false;
+    __device__ uint32_t count() const { return P.fluid_count; }
+    __device__ const DevParams& params(uint32_t) const { return P; }
+    __device__ Control* control(uint32_t) const { return ctl; }
+    __device__ bool skip_pressure(uint32_t) const { return false; }
+    __device__ bool skip_force(uint32_t) const { return false; }
+};
+
+// A batch: particle i belongs to scene scene_of[i]; per-scene parameters and control in device tables.
+struct SceneTable {
+    const DevParams* table;
+    Control* ctls;
+    const uint16_t* scene_of;
+    uint32_t n;          // particles of all scenes
+    uint32_t n_scenes;
+    static constexpr bool kBatched = true;
+    __device__ uint32_t count() const { return n; }
+    __device__ const DevParams& params(uint32_t i) const { return table[scene_of[i]]; }
+    __device__ Control* control(uint32_t i) const { return &ctls[scene_of[i]]; }
+    // the scene was decided done in an earlier iteration: no more pressure updates
+    __device__ bool skip_pressure(uint32_t i) const { return ctls[scene_of[i]].done != 0u; }
+    // the scene was integrated in an earlier iteration
+    __device__ bool skip_force(uint32_t i) const { return ctls[scene_of[i]].finished != 0u; }
+};
+
+void launch_density_list(const DevParams& P, Control* ctl, const ListBuffers& b, cudaStream_t s);
+void launch_normal_list(const DevParams& P, Control* ctl, const ListBuffers& b, cudaStream_t s);
+void launch_force_list(const DevParams& P, Control* ctl, const ListBuffers& b, cudaStream_t s);
+void launch_pressure_list(const DevParams& P, Control* ctl, const ListBuffers& b, cudaStream_t s);
+// mode 0: the loop decision picks predict or integrate; 1: predict; 2: integrate
+void launch_pressure_force_list(const DevParams& P, Control* ctl, const ListBuffers& b, int mode,
+                                cudaGraphConditionalHandle cond, bool use_cond, cudaStream_t s);
+
+void launch_batch_begin(Control* ctls, uint32_t n_scenes, Control* batch, cudaStream_t s);
+void launch_scene_of(const uint32_t* offsets, uint32_t n_scenes, uint32_t n, uint16_t* scene_of, cudaStream_t s);
+void launch_hash_scenes(const SceneTable& t, const float4* pos, uint32_t* keys, cudaStream_t s);
+void launch_density_scenes(const SceneTable& t, const ListBuffers& b, cudaStream_t s);
+void launch_normal_scenes(const SceneTable& t, const ListBuffers& b, cudaStream_t s);
+void launch_force_scenes(const SceneTable& t, const ListBuffers& b, cudaStream_t s);
+void launch_pressure_scenes(const SceneTable& t, const ListBuffers& b, cudaStream_t s);
+void launch_pressure_force_scenes(const SceneTable& t, const ListBuffers& b, cudaStream_t s);
+// per-scene loop decision; sets the while-loop condition (continue while a scene iterates)
+void launch_batch_decide(const SceneTable& t, Control* batch, int max_iters, cudaGraphConditionalHandle cond,
+                         bool use_cond, cudaStream_t s);
+
+}  // namespace pcisph

@@ -40,7 +40,7 @@ __global__ void __launch_bounds__(kBlock) k_hash(const float* __restrict__ pos, 
         x = p.x; y = p.y; z = p.z;
     }
     const Cell c = cell_of(x, y, z, P);
-    keys[i] = hash_key(c.x, c.y, c.z, P);
+    keys[i] = P.bucket_base + hash_key(c.x, c.y, c.z, P);
     if (ids) ids[i] = i;
 }
 

@@ -26,7 +26,6 @@ struct StepBuffers {
     uint32_t* groups;                // start of every bucket run (count in ctl->n_groups)
     uint32_t* nbr;                   // neighbour lists, list_cap entries per particle (kernel_variant 2)
     uint32_t* nbr_count;             // entries per particle; > list_cap means "walk the buckets"
-    uint32_t* work;                  // working order: particle handled by thread t (nullptr: identity)
     unsigned char* bucket_fast;      // per bucket: holds a particle predicted to move > skin / 2 (this step)
     // boundary
     float4 *b_pos, *bpf;
@@ -72,16 +71,6 @@ void launch_pressure_sweep(const DevParams& P, const StepBuffers& b, const Sweep
                            cudaStream_t s);
 void launch_pressure_force_sweep(const DevParams& P, const StepBuffers& b, const SweepArgs& A, const SweepGrid& g,
                                  int mode, cudaGraphConditionalHandle cond, bool use_cond, cudaStream_t s);
-
-// Neighbour-list sweeps (list_kernels.cu)
-void launch_morton(const float4* pos, uint32_t n, const DevParams& P, uint32_t* code, cudaStream_t s);
-void launch_iota(uint32_t* out, uint32_t n, cudaStream_t s);
-void launch_density_list(const DevParams& P, const StepBuffers& b, cudaStream_t s);
-void launch_normal_list(const DevParams& P, const StepBuffers& b, cudaStream_t s);
-void launch_force_list(const DevParams& P, const StepBuffers& b, cudaStream_t s);
-void launch_pressure_list(const DevParams& P, const StepBuffers& b, cudaStream_t s);
-void launch_pressure_force_list(const DevParams& P, const StepBuffers& b, int mode, cudaGraphConditionalHandle cond,
-                                bool use_cond, cudaStream_t s);
 
 void launch_pack3_to4(const float* in3, float4* out, uint32_t n, cudaStream_t s);
 void launch_unpack4_to3(const float4* in, float* out3, uint32_t n, cudaStream_t s);

@@ -77,7 +77,7 @@ __device__ __forceinline__ void sweep_subgroup(const DevParams& P, const Op& op,
     if (lane < 27) {
         const int dx = lane % 3 - 1, dy = (lane / 3) % 3 - 1, dz = lane / 9 - 1;
         const uint32_t x = cx + (uint32_t)dx, y = cy + (uint32_t)dy, z = cz + (uint32_t)dz;
-        const uint32_t key = hash_key(x, y, z, P);
+        const uint32_t key = P.bucket_base + hash_key(x, y, z, P);
         const uint2 r = __ldg(&A.cells[key]);
         fs = r.x;
         fl = r.y - r.x;

@@ -159,3 +159,69 @@ def boundary_box(lo, hi, d, layers=2):
                 if not inside:
                     pts.append((x, y, z))
     return np.asarray(pts, np.float32).reshape(-1, 3)
+
+
+def _lattice_points(nx, ny, nz, d, origin):
+    ix, iy, iz = np.meshgrid(np.arange(nx), np.arange(ny), np.arange(nz), indexing="ij")
+    idx = np.stack([ix.ravel(order="F"), iy.ravel(order="F"), iz.ravel(order="F")], 1).astype(np.float64)
+    return (idx + 0.5) * d + np.asarray(origin, np.float64)
+
+
+def _jitter(pos, seed, id_offset, d, jitter=0.05):
+    ids = np.arange(pos.shape[0], dtype=np.uint64) + np.uint64(id_offset)
+    out = pos.copy()
+    for a in range(3):
+        out[:, a] += (2.0 * uniform(seed, ids, a) - 1.0) * jitter * d
+    return out
+
+
+def batch_dam(count, aspect_x, aspect_z, d=0.01, seed=3, id_offset=0, delta_t=1e-3, name="dam"):
+    """A dam-break block of about `count` particles, sides nx:ny:nz = aspect_x:1:aspect_z, in a tank
+    2.5x as long and 2x as high as the block, as deep as the block."""
+    ny = max(2, int(round((count / (aspect_x * aspect_z)) ** (1.0 / 3.0))))
+    nx, nz = max(2, int(round(aspect_x * ny))), max(2, int(round(aspect_z * ny)))
+    pos = _jitter(_lattice_points(nx, ny, nz, d, (0.0, 0.0, 0.0)), seed, id_offset, d).astype(np.float32)
+    box_hi = (2.5 * nx * d, 2.0 * ny * d, nz * d)
+    return Scene(name, pos, d, delta_t, (0.0, 0.0, 0.0), box_hi)
+
+
+def batch_drop(count, d=0.01, seed=3, id_offset=0, delta_t=1e-3, drop_height=0.5, name="drop"):
+    """A fluid sphere of 70% of `count` particles whose bottom is `drop_height` above a pool holding the
+    other 30% in a square tank; the pool is half as deep as the sphere's radius, or shallower where the
+    tank must be wider than the sphere."""
+    n_sphere, n_pool = int(round(0.7 * count)), count - int(round(0.7 * count))
+    radius = (3.0 * n_sphere / (4.0 * np.pi)) ** (1.0 / 3.0) * d
+    pool_h = max(2 * d, 0.5 * radius)
+    side = max(4, int(round(np.sqrt(n_pool * d / pool_h))), int(np.ceil(2.0 * radius / d)) + 2)  # sphere fits
+    layers = max(1, int(round(n_pool / (side * side))))
+    pool = _lattice_points(side, layers, side, d, (0.0, 0.0, 0.0))
+    L = side * d
+    top = layers * d
+    centre = np.array([0.5 * L, top + drop_height + radius, 0.5 * L])
+    m = int(np.ceil(radius / d)) + 1
+    cube = _lattice_points(2 * m, 2 * m, 2 * m, d, centre - m * d)
+    sphere = cube[np.linalg.norm(cube - centre, axis=1) <= radius]
+    pos = np.concatenate([pool, sphere])
+    pos = _jitter(pos, seed, id_offset, d).astype(np.float32)
+    box_hi = (L, top + drop_height + 2.0 * radius + 2 * d, L)
+    return Scene(name, pos, d, delta_t, (0.0, 0.0, 0.0), box_hi)
+
+
+def config3_scenes(count=256, seed=3, n_min=4096, n_max=131072, d=0.01, delta_t=1e-3):
+    """Config 3: `count` scenes with log-uniform particle counts in [n_min, n_max]; each a dam-break block
+    (aspect ratios U[0.5, 2]) or a sphere dropped 0.5 m into a pool holding 30% of its particles."""
+    out, offset = [], 0
+    ids = np.arange(count, dtype=np.uint64)
+    u_n = uniform(seed, ids, 0, stream=1)
+    u_kind = uniform(seed, ids, 1, stream=1)
+    u_ax = uniform(seed, ids, 2, stream=1)
+    u_az = uniform(seed, ids, 3, stream=1)
+    for k in range(count):
+        n = int(round(np.exp(np.log(n_min) + u_n[k] * (np.log(n_max) - np.log(n_min)))))
+        if u_kind[k] < 0.5:
+            sc = batch_dam(n, 0.5 + 1.5 * u_ax[k], 0.5 + 1.5 * u_az[k], d, seed, offset, delta_t, f"dam{k}")
+        else:
+            sc = batch_drop(n, d, seed, offset, delta_t, name=f"drop{k}")
+        offset += sc.fluid_count
+        out.append(sc)
+    return out

@@ -1,0 +1,117 @@
+"""GPU: the batched multi-scene step (pcisph_batch_* C ABI) against the same scenes stepped alone.
+
+A scene in a batch sorts into its own bucket range of the shared cell table, keeps its relative particle
+order (the radix sort is stable), and walks the same neighbours in the same order with its own parameters;
+its loop decision uses its own threshold and limits. Its result must therefore be the result of the same
+scene in its own context, bit for bit: positions, velocities, densities and the iteration counts.
+"""
+import numpy as np
+import pytest
+
+from pcisph_gb300 import Batch, Fluid, scenes, setup_scene
+from pcisph_gb300._lib import PcisphError
+
+pytestmark = pytest.mark.gpu
+
+FIELDS = ("position", "velocity", "density", "pressure")
+
+
+def _mixed_scenes():
+    """Scenes of different sizes, shapes, spacings and loop settings."""
+    a = scenes.small_dam(8, seed=1)
+    b = scenes.small_dam(11, seed=2)
+    b.min_iters = b.max_iters = 4            # fixed iteration count
+    c = scenes.batch_dam(3000, 1.6, 0.7, d=0.01, seed=4)
+    c.threshold = 0.002                      # tighter: more iterations than the others
+    d = scenes.batch_drop(5000, d=0.01, seed=5)  # falls 0.5 m: fast particles near the pool
+    e = scenes.batch_dam(700, 0.6, 1.8, d=0.01, seed=6)
+    e.walls = False
+    return [a, b, c, d, e]
+
+
+def _alone(sc, steps):
+    f = Fluid(0)
+    setup_scene(f, sc, kernel_variant=2)
+    f.step(steps)
+    out = {n: f.get_field(n) for n in FIELDS}
+    st = f.stats()
+    return out, (st.iterations, st.steps, st.total_iterations, st.status_all)
+
+
+def _in_batch(bt, sid, sc):
+    out = {n: bt.get_field(sid, n, sc.fluid_count) for n in FIELDS}
+    st = bt.stats(sid)
+    return out, (st.iterations, st.steps, st.total_iterations, st.status_all)
+
+
+def _assert_same(name, got, want):
+    for n in FIELDS:
+        np.testing.assert_array_equal(got[0][n], want[0][n], err_msg=f"{name}: {n}")
+    assert got[1] == want[1], (name, got[1], want[1])
+
+
+def test_batch_scenes_match_alone():
+    sc = _mixed_scenes()
+    steps = 12
+    bt = Batch(0, max_particles=sum(s.fluid_count for s in sc) + 100, max_scenes=8)
+    ids = [bt.add_scene(s) for s in sc]
+    assert bt.info()[:2] == (len(sc), sum(s.fluid_count for s in sc))
+    bt.step(steps)
+    bt.sync()
+    iters = set()
+    for s, sid in zip(sc, ids):
+        got = _in_batch(bt, sid, s)
+        want = _alone(s, steps)
+        _assert_same(s.name, got, want)
+        iters.add(got[1][2])
+    assert len(iters) > 1  # the scenes did iterate differently
+    assert bt.kernel_launches() > 0
+
+
+def test_batch_remove_and_add_scenes():
+    sc = _mixed_scenes()
+    bt = Batch(0, max_particles=sum(s.fluid_count for s in sc), max_scenes=len(sc))
+    ids = [bt.add_scene(s) for s in sc[:4]]
+    bt.step(5)
+    bt.remove_scene(ids[1])  # compacts the later scenes and moves their statistics
+    with pytest.raises(PcisphError):
+        bt.stats(ids[1])
+    e_id = bt.add_scene(sc[4])
+    bt.step(4)
+    bt.sync()
+    for k in (0, 2, 3):
+        _assert_same(sc[k].name, _in_batch(bt, ids[k], sc[k]), _alone(sc[k], 9))
+    _assert_same(sc[4].name, _in_batch(bt, e_id, sc[4]), _alone(sc[4], 4))
+    assert bt.info()[0] == 4
+
+
+def test_batch_limits_and_errors():
+    a = scenes.small_dam(6, seed=1)
+    bt = Batch(0, max_particles=a.fluid_count * 2, max_scenes=2)
+    bt.step(1)  # empty batch: no-op
+    s0 = bt.add_scene(a)
+    bt.add_scene(a)
+    with pytest.raises(PcisphError):
+        bt.add_scene(a)  # no scene slot left
+    with pytest.raises(PcisphError):
+        bt.remove_scene(12345)
+    with pytest.raises(PcisphError):
+        bt.get_field(s0, "keys", a.fluid_count)
+    bt.remove_scene(s0)
+    big = scenes.small_dam(7, seed=1)
+    with pytest.raises(PcisphError):
+        bt.add_scene(big)  # more particles than are free
+    bt.step(2)
+    bt.sync()
+    assert bt.info()[:2] == (1, a.fluid_count)
+
+
+def test_batch_of_identical_scenes_is_identical():
+    a = scenes.batch_drop(3000, d=0.01, seed=8)
+    bt = Batch(0, max_particles=4 * a.fluid_count, max_scenes=4)
+    ids = [bt.add_scene(a) for _ in range(4)]
+    bt.step(6)
+    bt.sync()
+    first = _in_batch(bt, ids[0], a)
+    for sid in ids[1:]:
+        _assert_same("copy", _in_batch(bt, sid, a), first)

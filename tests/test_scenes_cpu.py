@@ -1,0 +1,33 @@
+"""CPU: the synthetic workloads (sizes, determinism) and the batch memory model."""
+import numpy as np
+
+from pcisph_gb300 import scenes
+from pcisph_gb300.batch import memory_model
+
+
+def test_config3_scenes_shape_and_determinism():
+    a = scenes.config3_scenes(count=64, seed=3)
+    b = scenes.config3_scenes(count=64, seed=3)
+    n = np.array([s.fluid_count for s in a])
+    assert len(a) == 64
+    assert n.min() >= 0.85 * 4096 and n.max() <= 1.1 * 131072
+    assert {s.name[:3] for s in a} == {"dam", "dro"}
+    for x, y in zip(a, b):
+        np.testing.assert_array_equal(x.fluid_pos, y.fluid_pos)
+    for s in a:  # every particle starts inside its tank
+        assert (s.fluid_pos >= np.asarray(s.box_lo) - s.spacing).all()
+        assert (s.fluid_pos <= np.asarray(s.box_hi) + s.spacing).all()
+
+
+def test_drop_scene_has_pool_and_sphere():
+    s = scenes.batch_drop(20000, d=0.01, seed=1)
+    y = s.fluid_pos[:, 1]
+    pool_top = np.sort(y)[int(0.3 * s.fluid_count) - 1]
+    gap = y[y > pool_top + 0.02]
+    assert 0.6 * s.fluid_count <= gap.size <= 0.72 * s.fluid_count
+    assert gap.min() - pool_top > 0.45  # dropped from 0.5 m above the pool
+
+
+def test_batch_memory_model():
+    per_particle, per_scene = memory_model()
+    assert 400 < per_particle < 1000 and per_scene > 0
