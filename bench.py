@@ -54,6 +54,14 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=20.0, help="bound of the CPU baseline sample")
     ap.add_argument("--variant", type=int, default=2, help="neighbour-sweep kernel variant (pcisph_options)")
+    ap.add_argument("--workload", default="dam1m", choices=["dam1m", "scenes", "serve"],
+                    help="dam1m: the 1M-particle dam break (the headline); scenes: 256 scenes batched vs "
+                         "stepped one context each; serve: Poisson requests through the serving loop")
+    ap.add_argument("--requests", type=int, default=20000, help="request count of --workload serve")
+    ap.add_argument("--rate", type=float, default=200.0, help="arrivals per second of --workload serve")
+    ap.add_argument("--budget-gb", type=float, default=100.0, help="device memory budget of --workload serve")
+    ap.add_argument("--duration", type=float, default=120.0, help="wall-time bound (s) of --workload serve")
+    ap.add_argument("--scenes", type=int, default=256, help="scene count of --workload scenes")
     return ap.parse_args()
 
 
@@ -70,8 +78,9 @@ def peaks():
         return 6800.0, "fallback"
 
 
-def ncu_traffic():
-    """Per-kernel DRAM bytes per particle from the committed ncu summary (profiles/ncu_traffic.txt)."""
+def ncu_traffic(variant):
+    """Per-kernel DRAM bytes per particle of one kernel variant, from the committed ncu summary
+    (profiles/ncu_traffic.txt)."""
     out = {}
     path = os.path.join(ROOT, "profiles", "ncu_traffic.txt")
     if not os.path.exists(path):
@@ -80,7 +89,8 @@ def ncu_traffic():
         for line in f:
             if line.startswith("kernel="):
                 kv = dict(tok.split("=", 1) for tok in line.split())
-                out[kv["kernel"]] = float(kv["dram_bytes_per_particle"])
+                if int(kv.get("variant", -1)) == variant:
+                    out[kv["kernel"]] = float(kv["dram_bytes_per_particle"])
     return out
 
 
@@ -179,11 +189,210 @@ def reference_arm(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+SCENES_WORKLOAD = ("256 scenes, particle counts log-uniform in [4,096, 131,072] (seed 3), each a dam-break block "
+                   "(aspect ratios U[0.5, 2]) or a sphere dropped 0.5 m into a pool holding 30% of its particles; "
+                   "d=0.01 m, dt=1e-3 s, reflecting walls, 3-50 corrective iterations to <1% density error per scene")
+
+
+def scenes_workload(args, rank, world, local):
+    """256 independent scenes: one batched step (pcisph_batch_*) against one context per scene, stepped one
+    after another on the same stream. Scenes shard across ranks (scene k on rank k mod N)."""
+    import numpy as np
+    import torch
+    import torch.distributed as dist
+
+    from pcisph_gb300 import Batch, Fluid, build, scenes, setup_scene
+    build.build()
+    all_sc = scenes.config3_scenes(count=args.scenes)
+    sc = all_sc[rank::world]
+    n_total = sum(s.fluid_count for s in sc)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    sampler = ClockSampler(local)
+    sampler.start()
+
+    def timed(step_fn, steps):
+        starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+        ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+        for k in range(steps):
+            starts[k].record(stream)
+            step_fn()
+            ends[k].record(stream)
+        torch.cuda.synchronize()
+        ms = sum(a.elapsed_time(b) for a, b in zip(starts, ends))
+        if world > 1:
+            t = torch.tensor([ms], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms
+
+    # batched: every scene in one pool, one graph launch per step
+    bt = Batch(local, max_particles=n_total, max_scenes=len(sc), stream=stream.cuda_stream)
+    ids = [bt.add_scene(s) for s in sc]
+    for _ in range(args.warmup):
+        bt.step(1)
+    bt.sync()
+    snap = [(bt.get_field(i, "position", s.fluid_count), bt.get_field(i, "velocity", s.fluid_count))
+            for i, s in zip(ids, sc)]
+    st0 = [bt.stats(i) for i in ids]
+    launches0 = bt.kernel_launches()
+    ms_batch = timed(lambda: bt.step(1), args.steps)
+    st1 = [bt.stats(i) for i in ids]
+    launches = bt.kernel_launches() - launches0
+    iters = [(b.total_iterations - a.total_iterations) / args.steps for a, b in zip(st0, st1)]
+    batch_loop_iters = max(iters)
+
+    # e2e through the batch ABI: host state of every scene in, one step, every scene's state out
+    e2e_steps = min(args.steps, 5)
+    pin = [(torch.empty((s.fluid_count, 3), dtype=torch.float32, pin_memory=True).numpy(),
+            torch.empty((s.fluid_count, 3), dtype=torch.float32, pin_memory=True).numpy()) for s in sc]
+    for (p, v), (p0, v0) in zip(pin, snap):
+        p[:] = p0
+        v[:] = v0
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        for i, (p, v) in zip(ids, pin):
+            bt.set_state(i, p, v)
+        bt.step(1)
+        for i, s, (p, v) in zip(ids, sc, pin):
+            p[:] = bt.get_field(i, "position", s.fluid_count)
+            v[:] = bt.get_field(i, "velocity", s.fluid_count)
+    e2e_s = time.perf_counter() - t0
+    bt.close()
+
+    # one context per scene, from the same state, each stepped once per step (graph launch each)
+    ctxs = []
+    for s, (p, v) in zip(sc, snap):
+        f = Fluid(local, stream=stream.cuda_stream)
+        setup_scene(f, s, kernel_variant=args.variant)
+        f.set_fluid_state(p, v)
+        ctxs.append(f)
+
+    def step_all():
+        for f in ctxs:
+            f.update()
+    ms_single = timed(step_all, args.steps)
+    single_launches = sum(f.kernel_launches() for f in ctxs)
+    for f in ctxs:
+        f.close()
+    clocks = sampler.stop()
+
+    cpu = None
+    if rank == 0 and world == 1:  # oracle on the smallest scenes, from the same state, bounded
+        order = np.argsort([s.fluid_count for s in sc])[:8]
+        done, t_cpu, cs = 0, 0.0, 0
+        for k in order:
+            r, steps_k, _, _ = cpu_step_rate(sc[k], snap[k][0], snap[k][1], args.cpu_seconds / 8, max_steps=args.steps)
+            done += sc[k].fluid_count * steps_k
+            t_cpu += sc[k].fluid_count * steps_k / r
+            cs += steps_k
+        cpu = {"value": done / t_cpu, "unit": "particle-steps/s", "cores": os.cpu_count(), "kind": "port",
+               "sample": f"the 8 smallest scenes, {cs} scene-steps from the timed loop's start state "
+                         f"(oracle/pcisph_oracle.cpp with OpenMP)"}
+    if rank == 0:
+        n_all = sum(s.fluid_count for s in all_sc)
+        value = n_all * args.steps / (ms_batch / 1e3)
+        line = {
+            "metric": "particle-steps/s, 256 scenes batched", "value": value, "unit": "particle-steps/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_batch / args.steps,
+            "higher_is_better": True, "scaling": "strong", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded scenes)",
+            "config": {"workload": SCENES_WORKLOAD, "scenes": len(all_sc), "particles": n_all,
+                       "parallelism": f"scenes sharded over {world} GPU(s)",
+                       "scene_steps_per_s": len(all_sc) * args.steps / (ms_batch / 1e3),
+                       "mean_scene_iterations": float(np.mean(iters)), "batch_loop_iterations": batch_loop_iters,
+                       "l2": "working set ~6 GB > L2"},
+            "per_scene_contexts": {"value": n_all * args.steps / (ms_single / 1e3), "unit": "particle-steps/s",
+                                   "ms_per_step": ms_single / args.steps, "gpu_launches": single_launches,
+                                   "speedup_of_batch": ms_single / ms_batch},
+            "e2e": {"value": n_total * e2e_steps * world / e2e_s, "unit": "particle-steps/s",
+                    "h2d_bytes_per_step": 24 * n_total, "d2h_bytes_per_step": 24 * n_total, "steps": e2e_steps},
+            "gpu_launches": launches, "cpu_baseline": cpu, "clocks": clocks,
+        }
+        print(json.dumps(line), flush=True)
+
+
+SERVE_WORKLOAD = ("Poisson arrivals; particle counts log-uniform in [2,048, 262,144], rollouts U[100, 1000] steps, "
+                  "scenes as the batched workload (seed 4); FIFO admission against a device-memory budget")
+
+
+def serve_workload(args, rank, world, local):
+    """The serving loop on live arrivals, bounded by --duration seconds of wall time. Requests shard over
+    ranks (request k on rank k mod N); each rank serves its share on its own pool."""
+    import torch
+    import torch.distributed as dist
+
+    from pcisph_gb300 import Batch, build
+    from pcisph_gb300.batch import memory_model
+    from pcisph_gb300.serve import Server, poisson_requests, shard
+    build.build()
+    # arrivals past the wall-time bound never reach the server: generate those that can
+    horizon = min(args.requests, int(args.rate * args.duration * 1.2) + 16)
+    reqs = shard(poisson_requests(horizon, args.rate, seed=4), rank, world)
+    bpp, bps = memory_model()
+    budget = int(args.budget_gb * (1 << 30))
+    max_particles = min(budget // bpp, (1 << 31) - 1)
+    max_scenes = min(65535, max(16, budget // (2048 * bpp + bps)))
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    bt = Batch(local, max_particles=max_particles, max_scenes=max_scenes, stream=stream.cuda_stream)
+    srv = Server(bt, budget, bpp, bps, max_particles, max_scenes, keep_state=True)
+    # warm-up: one small request served to completion before the clock starts (graph build, first launches)
+    Server(bt, budget, bpp, bps, max_particles, max_scenes, keep_state=False).run(reqs[:1], realtime=False)
+    sampler = ClockSampler(local)
+    sampler.start()
+    if world > 1:
+        dist.barrier()
+    rep = srv.run(reqs, duration=args.duration, realtime=True)
+    clocks = sampler.stop()
+    summ = rep.summary()
+    if world > 1:
+        got = [None] * world
+        dist.all_gather_object(got, summ)
+    else:
+        got = [summ]
+    if rank == 0:
+        wall = max(g["wall_s"] for g in got)
+        ps = sum(g["particle_steps_per_s"] * g["wall_s"] for g in got)
+        offered = sum(r.particles * r.steps for r in poisson_requests(min(horizon, 2000), args.rate, seed=4)) / \
+            min(horizon, 2000) * args.rate
+        line = {
+            "metric": "particle-steps/s served", "value": ps / wall, "unit": "particle-steps/s", "n_gpus": world,
+            "steps": summ["batch_steps"], "warmup": 1, "ms_per_step": summ["step_ms_p50"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded scenes, Poisson arrivals)",
+            "config": {"workload": SERVE_WORKLOAD, "rate_per_s": args.rate, "budget_gb": args.budget_gb,
+                       "duration_s": args.duration, "requests_generated": horizon,
+                       "offered_particle_steps_per_s": offered, "pool_particles": max_particles,
+                       "parallelism": f"requests sharded over {world} GPU(s)"},
+            "serve": got if world > 1 else summ,
+            "e2e": {"value": ps / wall, "unit": "particle-steps/s",
+                    "note": "every request's scene uploaded from host memory and its final state read back"},
+            "clocks": clocks,
+        }
+        print(json.dumps(line), flush=True)
+    bt.close()
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
     if args.impl == "reference":
         reference_arm(args, rank, world)
+        return
+    if args.workload in ("scenes", "serve"):
+        import torch
+        import torch.distributed as dist
+        if world > 1:
+            dist.init_process_group("gloo" if args.workload == "serve" else "nccl")
+        torch.cuda.set_device(local)
+        (scenes_workload if args.workload == "scenes" else serve_workload)(args, rank, world, local)
+        if world > 1:
+            dist.destroy_process_group()
         return
     import numpy as np
     import torch
@@ -257,7 +466,7 @@ def main():
     avg_s = dms / dl / 1e3
     peak, peak_kind = peaks()
     achieved = ALGO_BYTES.get(dname, 0) * N / avg_s / 1e9
-    traffic = ncu_traffic().get(dname)
+    traffic = ncu_traffic(args.variant).get(dname)
     kernels = {k: {"launches": l, "avg_us": 1e3 * ms / l, "share": ms / tot,
                    "algo_GBps": ALGO_BYTES.get(k, 0) * N / (ms / l / 1e3) / 1e9} for k, (l, ms) in prof.items()}
 

@@ -259,10 +259,13 @@ PCISPH_API int pcisph_batch_create(int device, void* stream, uint32_t max_partic
 PCISPH_API void pcisph_batch_destroy(pcisph_batch* batch);
 /* Bytes of device memory per particle and per scene in a pool (for admission against a budget). */
 PCISPH_API int pcisph_batch_memory_model(uint64_t* bytes_per_particle, uint64_t* bytes_per_scene);
-/* Adds a scene with its initial state (vel may be NULL: zero); *scene_id is a handle valid until removal. */
+/* Adds a scene with its initial state (vel may be NULL: zero); *scene_id is a handle valid until removal.
+ * The scene tables and the step's graph are rebuilt once, at the next step, for all additions and
+ * removals since the last step. */
 PCISPH_API int pcisph_batch_add_scene(pcisph_batch* batch, const pcisph_scene_desc* desc, const float* pos,
                                       const float* vel, int layout, int memory, int32_t* scene_id);
-/* Removes a scene; the pool is compacted (stream-ordered device copies). */
+/* Removes a scene: its id is invalid at once; its particles leave the pool at the next step, which compacts
+ * the pool once for all removals (stream-ordered device copies). */
 PCISPH_API int pcisph_batch_remove_scene(pcisph_batch* batch, int32_t scene_id);
 PCISPH_API int pcisph_batch_info(const pcisph_batch* batch, uint32_t* scenes, uint32_t* particles,
                                  uint32_t* free_particles);
@@ -271,6 +274,10 @@ PCISPH_API int pcisph_batch_step(pcisph_batch* batch, uint32_t steps);
 PCISPH_API int pcisph_batch_sync(pcisph_batch* batch);
 /* Synchronises, then reports the scene's last step (and totals since it was added). */
 PCISPH_API int pcisph_batch_scene_stats(pcisph_batch* batch, int32_t scene_id, pcisph_step_stats* out);
+/* Replaces a scene's positions (and velocities; NULL: zero), as pcisph_set_fluid_state; count must be the
+ * scene's particle count. The scene keeps its parameters, statistics and place in the pool. */
+PCISPH_API int pcisph_batch_set_state(pcisph_batch* batch, int32_t scene_id, const float* pos, const float* vel,
+                                      uint32_t count, int layout, int memory);
 /* A field of one scene (its particles in its own sorted order), as pcisph_get_field. */
 PCISPH_API int pcisph_batch_get_field(pcisph_batch* batch, int32_t scene_id, int field, void* dst,
                                       size_t dst_bytes, int layout, int memory);

@@ -151,6 +151,7 @@ def load():
         "pcisph_batch_sync": ([vp], i32),
         "pcisph_batch_scene_stats": ([vp, C.c_int32, C.POINTER(StepStats)], i32),
         "pcisph_batch_get_field": ([vp, C.c_int32, i32, vp, sz, i32, i32], i32),
+        "pcisph_batch_set_state": ([vp, C.c_int32, vp, vp, C.c_uint32, i32, i32], i32),
         "pcisph_batch_kernel_launches": ([vp], C.c_uint64),
     }
     for name, (args, res) in sig.items():

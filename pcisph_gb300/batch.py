@@ -70,6 +70,17 @@ class Batch:
                                              _lib.MEM_HOST, C.byref(sid)))
         return sid.value
 
+    def set_state(self, sid, pos, vel=None):
+        """Replace a scene's state from host arrays ((n, 3) or (n, 4) float32; vel None: zero)."""
+        pos = np.ascontiguousarray(pos, np.float32)
+        vel = None if vel is None else np.ascontiguousarray(vel, np.float32)
+        layout = _lib.LAYOUT_FLOAT4 if pos.shape[1] == 4 else _lib.LAYOUT_PACKED3
+        if vel is not None and vel.shape != pos.shape:
+            raise ValueError("positions and velocities differ in shape")
+        check(self._L.pcisph_batch_set_state(self._h, int(sid), C.c_void_p(pos.ctypes.data),
+                                             None if vel is None else C.c_void_p(vel.ctypes.data),
+                                             pos.shape[0], layout, _lib.MEM_HOST))
+
     def remove_scene(self, sid):
         check(self._L.pcisph_batch_remove_scene(self._h, int(sid)))
 

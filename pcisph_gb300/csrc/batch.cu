@@ -38,9 +38,10 @@ struct SceneSlot {
     pcisph_scene_desc desc;
     pcisph_sim_params params;
     uint32_t offset, count, bucket_base;
+    bool removed;  // dropped at the next compaction
 };
 
-constexpr size_t kParticleBytes = 10 * 16 + 3 * 4 + 2 * 4 + 2 + kListCap * 4 + 4 + 16;  // arrays + staging
+constexpr size_t kParticleBytes = 11 * 16 + 3 * 4 + 4 * 4 + 2 + kListCap * 4;  // the pool arrays of allocate()
 constexpr size_t kBucketBytesPerParticle = 5;  // (8 B table + 1 B flag) per bucket, ~N/2 buckets
 
 }  // namespace
@@ -67,6 +68,7 @@ struct pcisph_batch {
     int32_t next_id = 1;
     uint32_t n_particles = 0, n_buckets = 0;
     int max_iters = 1;
+    bool dirty = false;  // scenes were added or removed since the tables were built
     cudaGraphExec_t graph_exec = nullptr;
     bool graph_valid = false;
     uint64_t host_launches = 0;
@@ -140,7 +142,60 @@ struct pcisph_batch {
                            cells, cells, nullptr, nullptr, nbr, nbr_count, bucket_fast};
     }
 
-    // Scene tables after a change of composition: bucket ranges, parameters, offsets, particle -> scene.
+    uint32_t pool_end() const { return scenes.empty() ? 0u : scenes.back().offset + scenes.back().count; }
+    uint32_t live_scenes() const {
+        uint32_t n = 0;
+        for (const SceneSlot& sl : scenes) n += sl.removed ? 0u : 1u;
+        return n;
+    }
+    uint32_t live_particles() const {
+        uint32_t n = 0;
+        for (const SceneSlot& sl : scenes) n += sl.removed ? 0u : sl.count;
+        return n;
+    }
+
+    // Drops the removed scenes: the later scenes move down (through the sorted-order arrays, which are free
+    // between steps) and their control records with them. Then the scene tables are rebuilt.
+    int compact() {
+        cudaStream_t st = stream();
+        size_t first = scenes.size();
+        for (size_t k = 0; k < scenes.size(); ++k)
+            if (scenes[k].removed) {
+                first = k;
+                break;
+            }
+        if (first < scenes.size()) {
+            std::vector<SceneSlot> kept(scenes.begin(), scenes.begin() + first);
+            std::vector<size_t> ctl_src;
+            const uint32_t from = scenes[first].offset;
+            uint32_t off = from;
+            for (size_t k = first; k < scenes.size(); ++k) {
+                const SceneSlot& sl = scenes[k];
+                if (sl.removed) continue;
+                BTRY(cudaMemcpyAsync(pos + off, state_pos + sl.offset, (size_t)sl.count * 16, cudaMemcpyDeviceToDevice, st));
+                BTRY(cudaMemcpyAsync(vel + off, state_vel + sl.offset, (size_t)sl.count * 16, cudaMemcpyDeviceToDevice, st));
+                ctl_src.push_back(k);
+                kept.push_back(sl);
+                off += sl.count;
+            }
+            if (off > from) {
+                BTRY(cudaMemcpyAsync(state_pos + from, pos + from, (size_t)(off - from) * 16, cudaMemcpyDeviceToDevice, st));
+                BTRY(cudaMemcpyAsync(state_vel + from, vel + from, (size_t)(off - from) * 16, cudaMemcpyDeviceToDevice, st));
+            }
+            if (!ctl_src.empty()) {  // per-scene statistics move with their scenes
+                BTRY(cudaMemcpyAsync(h_ctls, d_ctls, scenes.size() * sizeof(Control), cudaMemcpyDeviceToHost, st));
+                BTRY(cudaStreamSynchronize(st));
+                for (size_t j = 0; j < ctl_src.size(); ++j) h_ctls[first + j] = h_ctls[ctl_src[j]];  // src >= dst
+                BTRY(cudaMemcpyAsync(d_ctls + first, h_ctls + first, ctl_src.size() * sizeof(Control),
+                                     cudaMemcpyHostToDevice, st));
+            }
+            scenes.swap(kept);
+        }
+        return rebuild();
+    }
+
+    // Scene tables after a change of composition (scenes packed from offset 0): bucket ranges, parameters,
+    // offsets, particle -> scene.
     int rebuild() {
         std::vector<DevParams> table(scenes.size());
         std::vector<uint32_t> offsets(scenes.size() + 1);
@@ -171,6 +226,7 @@ struct pcisph_batch {
         }
         BTRY(cudaStreamSynchronize(st));  // the host vectors above go out of scope
         graph_valid = false;
+        dirty = false;
         return PCISPH_OK;
     }
 
@@ -246,6 +302,10 @@ struct pcisph_batch {
     }
 
     int step(uint32_t steps) {
+        if (dirty) {
+            int rc = compact();
+            if (rc) return rc;
+        }
         if (scenes.empty()) return PCISPH_OK;
         if (!graph_valid) {
             int rc = build_graph();
@@ -260,7 +320,7 @@ struct pcisph_batch {
 
     int find(int32_t id) const {
         for (size_t k = 0; k < scenes.size(); ++k)
-            if (scenes[k].id == id) return (int)k;
+            if (scenes[k].id == id && !scenes[k].removed) return (int)k;
         return -1;
     }
 
@@ -288,7 +348,7 @@ struct pcisph_batch {
 extern "C" {
 
 int pcisph_batch_memory_model(uint64_t* bytes_per_particle, uint64_t* bytes_per_scene) {
-    if (bytes_per_particle) *bytes_per_particle = kParticleBytes + kBucketBytesPerParticle + 48;  // + sort scratch
+    if (bytes_per_particle) *bytes_per_particle = kParticleBytes + kBucketBytesPerParticle + 12;  // + sort scratch
     if (bytes_per_scene) *bytes_per_scene = sizeof(DevParams) + sizeof(Control) + 4 + 64 * 9;
     return PCISPH_OK;
 }
@@ -335,19 +395,25 @@ int pcisph_batch_add_scene(pcisph_batch* b, const pcisph_scene_desc* d, const fl
         return report_error(PCISPH_ERR_INVALID_ARG, "positions take PACKED3 or FLOAT4");
     if (d->min_iterations < 1 || d->max_iterations < 1 || d->max_iterations > 10000)
         return report_error(PCISPH_ERR_INVALID_ARG, "iteration limits must be in 1..10000");
-    if (b->scenes.size() >= b->max_scenes) return report_error(PCISPH_ERR_OOM, "batch is full (max_scenes)");
-    if ((uint64_t)b->n_particles + d->fluid_count > b->max_particles)
+    if (b->live_scenes() >= b->max_scenes) return report_error(PCISPH_ERR_OOM, "batch is full (max_scenes)");
+    if ((uint64_t)b->live_particles() + d->fluid_count > b->max_particles)
         return report_error(PCISPH_ERR_OOM, "batch is full (max_particles)");
     DeviceGuard g(b->device);
+    if (b->scenes.size() >= b->max_scenes || (uint64_t)b->pool_end() + d->fluid_count > b->max_particles) {
+        int rc = b->compact();  // make room: drop the removed scenes now
+        if (rc) return rc;
+    }
     SceneSlot s{};
     s.id = b->next_id++;
     s.desc = *d;
     s.count = d->fluid_count;
     pcisph_derive_params(d->particle_radius, d->rest_density, d->fluid_count, 0, d->delta_t, d->gravity, d->viscosity,
                          d->surface_tension, &s.params);
-    if ((uint64_t)b->n_buckets + s.params.bucket_count > b->max_buckets)
-        return report_error(PCISPH_ERR_OOM, "batch is full (buckets)");
-    const uint32_t off = b->n_particles;
+    uint64_t buckets = s.params.bucket_count;
+    for (const SceneSlot& sl : b->scenes) buckets += sl.removed ? 0u : sl.params.bucket_count;
+    if (buckets > b->max_buckets) return report_error(PCISPH_ERR_OOM, "batch is full (buckets)");
+    const uint32_t off = b->pool_end();
+    s.offset = off;
     int rc = b->copy_in(b->state_pos + off, pos, s.count, layout, memory);
     if (!rc && vel) rc = b->copy_in(b->state_vel + off, vel, s.count, layout, memory);
     else if (!rc) BTRY(cudaMemsetAsync(b->state_vel + off, 0, (size_t)s.count * 16, b->stream()));
@@ -355,41 +421,44 @@ int pcisph_batch_add_scene(pcisph_batch* b, const pcisph_scene_desc* d, const fl
     const size_t k = b->scenes.size();
     BTRY(cudaMemsetAsync(b->d_ctls + k, 0, sizeof(Control), b->stream()));
     b->scenes.push_back(s);
-    rc = b->rebuild();
-    if (rc) return rc;
+    b->dirty = true;  // tables and graph are rebuilt by the next step
     *scene_id = s.id;
     return PCISPH_OK;
+}
+
+int pcisph_batch_set_state(pcisph_batch* b, int32_t id, const float* pos, const float* vel, uint32_t count,
+                           int layout, int memory) {
+    if (!b || !pos) return report_error(PCISPH_ERR_INVALID_ARG, "NULL argument");
+    if (layout != PCISPH_LAYOUT_PACKED3 && layout != PCISPH_LAYOUT_FLOAT4)
+        return report_error(PCISPH_ERR_INVALID_ARG, "positions take PACKED3 or FLOAT4");
+    const int k = b->find(id);
+    if (k < 0) return report_error(PCISPH_ERR_INVALID_ARG, "unknown scene id " + std::to_string(id));
+    const SceneSlot& s = b->scenes[k];
+    if (count != s.count)
+        return report_error(PCISPH_ERR_INCONSISTENT, "scene " + std::to_string(id) + " has " + std::to_string(s.count) +
+                                                         " particles, not " + std::to_string(count));
+    DeviceGuard g(b->device);
+    int rc = b->copy_in(b->state_pos + s.offset, pos, s.count, layout, memory);
+    if (!rc && vel) rc = b->copy_in(b->state_vel + s.offset, vel, s.count, layout, memory);
+    else if (!rc) BTRY(cudaMemsetAsync(b->state_vel + s.offset, 0, (size_t)s.count * 16, b->stream()));
+    return rc;
 }
 
 int pcisph_batch_remove_scene(pcisph_batch* b, int32_t id) {
     if (!b) return report_error(PCISPH_ERR_INVALID_ARG, "batch is NULL");
     const int k = b->find(id);
     if (k < 0) return report_error(PCISPH_ERR_INVALID_ARG, "unknown scene id " + std::to_string(id));
-    DeviceGuard g(b->device);
-    cudaStream_t s = b->stream();
-    const SceneSlot gone = b->scenes[k];
-    const uint32_t tail = gone.offset + gone.count, tail_n = b->n_particles - tail;
-    if (tail_n) {  // move the later scenes down through scratch arrays (the ranges may overlap)
-        BTRY(cudaMemcpyAsync(b->pos, b->state_pos + tail, (size_t)tail_n * 16, cudaMemcpyDeviceToDevice, s));
-        BTRY(cudaMemcpyAsync(b->vel, b->state_vel + tail, (size_t)tail_n * 16, cudaMemcpyDeviceToDevice, s));
-        BTRY(cudaMemcpyAsync(b->state_pos + gone.offset, b->pos, (size_t)tail_n * 16, cudaMemcpyDeviceToDevice, s));
-        BTRY(cudaMemcpyAsync(b->state_vel + gone.offset, b->vel, (size_t)tail_n * 16, cudaMemcpyDeviceToDevice, s));
-    }
-    const size_t later = b->scenes.size() - (size_t)k - 1;
-    if (later) {  // per-scene statistics move with their scenes
-        BTRY(cudaMemcpyAsync(b->h_ctls, b->d_ctls + k + 1, later * sizeof(Control), cudaMemcpyDeviceToHost, s));
-        BTRY(cudaStreamSynchronize(s));
-        BTRY(cudaMemcpyAsync(b->d_ctls + k, b->h_ctls, later * sizeof(Control), cudaMemcpyHostToDevice, s));
-    }
-    b->scenes.erase(b->scenes.begin() + k);
-    return b->rebuild();
+    b->scenes[k].removed = true;  // compacted with every other removal at the next step
+    b->dirty = true;
+    return PCISPH_OK;
 }
 
 int pcisph_batch_info(const pcisph_batch* b, uint32_t* scenes, uint32_t* particles, uint32_t* free_particles) {
     if (!b) return report_error(PCISPH_ERR_INVALID_ARG, "batch is NULL");
-    if (scenes) *scenes = (uint32_t)b->scenes.size();
-    if (particles) *particles = b->n_particles;
-    if (free_particles) *free_particles = b->max_particles - b->n_particles;
+    const uint32_t live = b->live_particles();
+    if (scenes) *scenes = b->live_scenes();
+    if (particles) *particles = live;
+    if (free_particles) *free_particles = b->max_particles - live;
     return PCISPH_OK;
 }
 
