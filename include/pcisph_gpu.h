@@ -93,6 +93,9 @@ typedef struct pcisph_options {
                                       0: one warp per bucket run with shared-memory staging; 1: one thread per
                                       particle walking the 27 buckets in every sweep */
     float list_skin;               /* variant 2: list radius = kernel_radius * (1 + list_skin), default 0.25 */
+    int32_t spatial_order;         /* variant 2, default 1: the sweeps run in a working order that places
+                                      whole buckets in Morton order of their cells (every sum unchanged; state
+                                      and exported fields stay in the reference's sorted order); 0: sorted order */
 } pcisph_options;
 
 typedef struct pcisph_step_stats {

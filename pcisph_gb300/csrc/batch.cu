@@ -139,7 +139,7 @@ struct pcisph_batch {
     }
     ListBuffers list_buffers() const {
         return ListBuffers{pos, vel, pr4, normal, f_other, f_press, pred, pf4, state_pos, state_vel, rho, press, err,
-                           cells, cells, nullptr, nullptr, nbr, nbr_count, bucket_fast};
+                           cells, cells, nullptr, nullptr, nbr, nbr_count, bucket_fast, n_particles, nullptr};
     }
 
     uint32_t pool_end() const { return scenes.empty() ? 0u : scenes.back().offset + scenes.back().count; }
@@ -356,8 +356,8 @@ int pcisph_batch_memory_model(uint64_t* bytes_per_particle, uint64_t* bytes_per_
 int pcisph_batch_create(int device, void* stream, uint32_t max_particles, uint32_t max_scenes, pcisph_batch** out) {
     if (!out) return report_error(PCISPH_ERR_INVALID_ARG, "out is NULL");
     *out = nullptr;
-    if (max_particles == 0 || max_scenes == 0 || max_scenes > 65535)
-        return report_error(PCISPH_ERR_INVALID_ARG, "max_particles must be > 0 and max_scenes in 1..65535");
+    if (max_particles == 0 || max_particles >= (1u << 31) || max_scenes == 0 || max_scenes > 65535)
+        return report_error(PCISPH_ERR_INVALID_ARG, "max_particles must be in 1..2^31-1 and max_scenes in 1..65535");
     int ndev = 0;
     BTRY(cudaGetDeviceCount(&ndev));
     if (device < 0 || device >= ndev) return report_error(PCISPH_ERR_INVALID_ARG, "no CUDA device " + std::to_string(device));

@@ -26,6 +26,7 @@
 #include "radix_sort.cuh"
 #include "host_util.h"
 #include "list_kernels.cuh"
+#include "spatial_order.cuh"
 #include "step_kernels.cuh"
 #include "sweep.cuh"
 
@@ -74,7 +75,17 @@ struct pcisph_ctx {
     uint32_t fluid_loaded = 0xFFFFFFFFu, boundary_loaded = 0xFFFFFFFFu;
     uint32_t fluid_cap_n = 0, fluid_cap_bk = 0, boundary_cap_n = 0, boundary_cap_bk = 0;
 
-    DeviceBlock fluid_block, boundary_block, misc_block, sort_block, staging_block, list_block;
+    DeviceBlock fluid_block, boundary_block, misc_block, sort_block, staging_block, list_block, order_block,
+        bucket_sort_block;
+    // working order (variant 2 with spatial_order): bucket ranges in working order, bucket Morton codes,
+    // the two index maps, scan scratch, and a transfer buffer for fields exported or imported in sorted order
+    uint2* cells_w = nullptr;
+    uint32_t *bucket_codes = nullptr, *bucket_ids = nullptr, *d_of_w = nullptr, *w_of_d = nullptr;
+    uint32_t* range_scratch = nullptr;
+    float4* xfer = nullptr;
+    RadixSorter bucket_sorter;
+    size_t order_n = 0, order_bk = 0;
+    std::map<int, DeviceBlock> exports;  // sorted-order copies handed out by pcisph_field_device_ptr
     StepBuffers b{};
     float4* b_pos_in = nullptr;
     uint32_t *f_keys = nullptr, *f_ids = nullptr, *b_keys = nullptr, *b_ids = nullptr;
@@ -91,15 +102,89 @@ struct pcisph_ctx {
     }
     bool warp_sweeps() const { return opts.kernel_variant == 0; }
     bool list_sweeps() const { return opts.kernel_variant == 2; }
+    bool working_order() const { return list_sweeps() && opts.spatial_order != 0; }
     ListBuffers list_buffers() const {
+        const bool w = working_order();
         return ListBuffers{b.pos, b.vel, b.pr4, b.normal, b.f_other, b.f_press, b.pred, b.pf4, b.state_pos,
-                           b.state_vel, b.rho, b.press, b.err, b.cells, b.b_cells, b.b_pos, b.bpf, b.nbr,
-                           b.nbr_count, b.bucket_fast};
+                           b.state_vel, b.rho, b.press, b.err, w ? cells_w : b.cells, b.b_cells, b.b_pos, b.bpf,
+                           b.nbr, b.nbr_count, b.bucket_fast, P.fluid_count, w ? d_of_w : nullptr};
+    }
+
+    // Working-order buffers for n particles and bk buckets; the index maps start as the identity.
+    int ensure_order() {
+        if (!working_order()) return PCISPH_OK;
+        const size_t n = params.fluid_count, bk = params.bucket_count;
+        if (order_block.p && order_n == n && order_bk == bk) return PCISPH_OK;
+        CUDA_TRY(cudaStreamSynchronize(stream()));
+        const size_t bytes = align256(bk * 8) + 2 * align256(bk * 4) + 2 * align256(n * 4) +
+                             align256(working_ranges_scratch((uint32_t)bk) * 4) + align256(n * 16);
+        if (order_block.ensure(bytes) != cudaSuccess)
+            return fail(PCISPH_ERR_OOM, "device allocation of the working-order buffers failed");
+        Carver c{static_cast<unsigned char*>(order_block.p)};
+        cells_w = c.take<uint2>(bk);
+        bucket_codes = c.take<uint32_t>(bk);
+        bucket_ids = c.take<uint32_t>(bk);
+        d_of_w = c.take<uint32_t>(n);
+        w_of_d = c.take<uint32_t>(n);
+        range_scratch = c.take<uint32_t>(working_ranges_scratch((uint32_t)bk));
+        xfer = c.take<float4>(n);
+        bucket_sorter.set_digit_bits(10);
+        const size_t sbytes = RadixSorter::scratch_bytes(bk, 10);
+        if (bucket_sort_block.ensure(sbytes) != cudaSuccess)
+            return fail(PCISPH_ERR_OOM, "device allocation of the bucket-sort scratch failed");
+        bucket_sorter.set_scratch(bucket_sort_block.p, bucket_sort_block.cap);
+        launch_iota(d_of_w, (uint32_t)n, stream());
+        launch_iota(w_of_d, (uint32_t)n, stream());
+        host_launches += 2;
+        CUDA_TRY(cudaGetLastError());
+        order_n = n;
+        order_bk = bk;
+        graph_valid = false;
+        return PCISPH_OK;
+    }
+
+    // After the hash sort (sorted keys sk, ids sv): the reference's cell table, then the working order and
+    // the particles gathered into it. Returns the launches issued, or -1.
+    int record_working_order(const uint32_t* sk, const uint32_t* sv, cudaStream_t s) {
+        const uint32_t N = params.fluid_count, BK = params.bucket_count;
+        if (cudaMemsetAsync(bucket_codes, 0xFF, (size_t)BK * 4, s) != cudaSuccess) return -1;
+        int nl = 0;
+        timed("reorder", s, [&] { launch_bucket_codes(sk, sv, b.state_pos, N, P, b.cells, bucket_codes, b.ctl, s); });
+        ++nl;
+        uint32_t *ok = nullptr, *order = nullptr;
+        cudaError_t e = cudaSuccess;
+        timed("bucket_sort", s, [&] {
+            e = bucket_sorter.sort(bucket_codes, bucket_ids, BK, 30, true, s, &ok, &order);
+            nl += bucket_sorter.last_launches();
+        });
+        if (e != cudaSuccess) return -1;
+        timed("working_ranges", s, [&] { launch_working_ranges(order, BK, b.cells, cells_w, range_scratch, N, s); });
+        timed("permute", s, [&] {
+            launch_permute(sk, sv, b.state_pos, b.state_vel, N, BK, b.cells, cells_w, b.pos, b.vel, d_of_w, w_of_d,
+                           b.ctl, s);
+        });
+        nl += 4;
+        return cudaGetLastError() == cudaSuccess ? nl : -1;
+    }
+
+    // Fields stored in working order while the working order is on (the state arrays are in sorted order).
+    bool in_working_order(int field) const {
+        if (!working_order() || !w_of_d) return false;
+        switch (field) {
+            case PCISPH_FIELD_NORMAL: case PCISPH_FIELD_PREDICTED_POSITION: case PCISPH_FIELD_DENSITY:
+            case PCISPH_FIELD_OTHER_FORCE: case PCISPH_FIELD_PRESSURE: case PCISPH_FIELD_PRESSURE_FORCE:
+            case PCISPH_FIELD_DENSITY_VARIATION: case PCISPH_FIELD_SORTED_POSITION:
+            case PCISPH_FIELD_SORTED_VELOCITY:
+                return true;
+            default:
+                return false;
+        }
     }
 
     int ensure_lists() {
         if (!list_sweeps()) return PCISPH_OK;
         const size_t n = params.fluid_count;
+        if (n >= (1u << 31)) return fail(PCISPH_ERR_INVALID_ARG, "kernel variant 2 takes fewer than 2^31 particles");
         const size_t bytes = align256(n * P.list_cap * 4) + align256(n * 4) + align256(params.bucket_count);
         if (list_block.p && list_block.cap >= bytes && list_n == n) return PCISPH_OK;
         CUDA_TRY(cudaStreamSynchronize(stream()));
@@ -316,7 +401,13 @@ struct pcisph_ctx {
         nl += r;
         sorted_keys = sk;
         sorted_ids = sv;
-        timed("reorder", s, [&] { launch_reorder(sk, sv, b.state_pos, b.state_vel, N, b.pos, b.vel, b.cells, b.codes, b.groups, P, b.ctl, s); });
+        if (working_order()) {
+            const int r2 = record_working_order(sk, sv, s);
+            if (r2 < 0) return -1;
+            nl += r2 - 1;  // the reorder launch is counted below
+        } else {
+            timed("reorder", s, [&] { launch_reorder(sk, sv, b.state_pos, b.state_vel, N, b.pos, b.vel, b.cells, b.codes, b.groups, P, b.ctl, s); });
+        }
         const SweepArgs A = sweep_args();
         if (list_sweeps()) {
             timed("density", s, [&] { launch_density_list(P, b.ctl, list_buffers(), s); });
@@ -429,6 +520,7 @@ struct pcisph_ctx {
         if (rc) return rc;
         if (params.fluid_count == 0) return PCISPH_OK;  // Fluid.cpp:117-118
         rc = ensure_lists();
+        if (!rc) rc = ensure_order();
         if (rc) return rc;
         cudaStream_t s = stream();
         if (boundary_updated && params.boundary_count > 0) {
@@ -473,6 +565,7 @@ struct pcisph_ctx {
         int rc = check_consistent();
         if (rc) return rc;
         rc = ensure_lists();
+        if (!rc) rc = ensure_order();
         if (rc) return rc;
         cudaStream_t s = stream();
         const uint32_t N = params.fluid_count;
@@ -490,8 +583,14 @@ struct pcisph_ctx {
                 if (nl < 0) return PCISPH_ERR_CUDA;
                 sorted_keys = sk;
                 sorted_ids = sv;
-                launch_reorder(sk, sv, b.state_pos, b.state_vel, N, b.pos, b.vel, b.cells, b.codes, b.groups, P, b.ctl, s);
-                host_launches += nl + 2;
+                if (working_order()) {
+                    const int r2 = record_working_order(sk, sv, s);
+                    if (r2 < 0) return fail(PCISPH_ERR_CUDA, "working order of the sort stage failed");
+                    host_launches += nl + 1 + r2;
+                } else {
+                    launch_reorder(sk, sv, b.state_pos, b.state_vel, N, b.pos, b.vel, b.cells, b.codes, b.groups, P, b.ctl, s);
+                    host_launches += nl + 2;
+                }
                 break;
             }
             case PCISPH_STAGE_DENSITY:
@@ -607,6 +706,15 @@ struct pcisph_ctx {
         if (need == 0) return PCISPH_OK;
         cudaStream_t s = stream();
         const cudaMemcpyKind kind = memory == PCISPH_MEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+        if (in_working_order(field)) {  // back to sorted order: out[d] = field[w_of_d[d]]
+            if (v.layout == PCISPH_LAYOUT_FLOAT4)
+                launch_gather4(static_cast<const float4*>(v.ptr), w_of_d, xfer, (uint32_t)v.count, s);
+            else
+                launch_gather1(static_cast<const float*>(v.ptr), w_of_d, reinterpret_cast<float*>(xfer), (uint32_t)v.count, s);
+            ++host_launches;
+            CUDA_TRY(cudaGetLastError());
+            v.ptr = xfer;
+        }
         if (layout == PCISPH_LAYOUT_PACKED3) {
             float* out = memory == PCISPH_MEM_HOST ? static_cast<float*>(staging_block.p) : static_cast<float*>(dst);
             launch_unpack4_to3(static_cast<const float4*>(v.ptr), out, (uint32_t)v.count, s);
@@ -626,6 +734,23 @@ struct pcisph_ctx {
         if (!v.ptr) return fail(PCISPH_ERR_NOT_READY, "field not allocated yet");
         const size_t need = layout_bytes(v.count, layout);
         if (src_bytes < need || (!src && need)) return fail(PCISPH_ERR_INVALID_ARG, "source too small");
+        if (in_working_order(field) && v.count) {  // sorted order in, working order stored: f[w_of_d[d]] = in[d]
+            cudaStream_t s = stream();
+            if (v.layout == PCISPH_LAYOUT_FLOAT4) {
+                int rc = copy_vectors_in(xfer, static_cast<const float*>(src), v.count, layout, memory);
+                if (rc) return rc;
+                launch_scatter4(xfer, w_of_d, static_cast<float4*>(v.ptr), (uint32_t)v.count, s);
+            } else {
+                if (layout != PCISPH_LAYOUT_SCALAR) return fail(PCISPH_ERR_INVALID_ARG, "scalar field: use PCISPH_LAYOUT_SCALAR");
+                CUDA_TRY(cudaMemcpyAsync(xfer, src, need,
+                                         memory == PCISPH_MEM_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice, s));
+                launch_scatter1(reinterpret_cast<const float*>(xfer), w_of_d, static_cast<float*>(v.ptr), (uint32_t)v.count, s);
+            }
+            ++host_launches;
+            CUDA_TRY(cudaGetLastError());
+            if (memory == PCISPH_MEM_HOST) CUDA_TRY(cudaStreamSynchronize(s));
+            return PCISPH_OK;
+        }
         if (v.layout == PCISPH_LAYOUT_FLOAT4)
             return copy_vectors_in(static_cast<float4*>(v.ptr), static_cast<const float*>(src), v.count, layout, memory);
         if (layout != PCISPH_LAYOUT_SCALAR) return fail(PCISPH_ERR_INVALID_ARG, "scalar field: use PCISPH_LAYOUT_SCALAR");
@@ -665,6 +790,9 @@ struct pcisph_ctx {
         sort_block.release();
         staging_block.release();
         list_block.release();
+        order_block.release();
+        bucket_sort_block.release();
+        for (auto& kv : exports) kv.second.release();
         if (host_ctl) cudaFreeHost(host_ctl);
         if (capture_stream) cudaStreamDestroy(capture_stream);
         if (own_stream) cudaStreamDestroy(own_stream);
@@ -712,6 +840,7 @@ int pcisph_default_options(pcisph_options* o) {
     o->loop_mode = 0;
     o->kernel_variant = 2;
     o->list_skin = 0.25f;
+    o->spatial_order = 1;
     return PCISPH_OK;
 }
 
@@ -928,6 +1057,17 @@ int pcisph_field_device_ptr(pcisph_ctx* ctx, int field, void** ptr, size_t* coun
     if (!ctx || !ptr) return fail(PCISPH_ERR_INVALID_ARG, "NULL argument");
     pcisph_ctx::FieldView v;
     if (!ctx->field_view(field, &v)) return fail(PCISPH_ERR_INVALID_ARG, "unknown field");
+    if (ctx->in_working_order(field) && v.ptr && v.count) {  // a sorted-order copy, made now (stream-ordered)
+        DeviceGuard g(ctx->device);
+        const size_t esz = v.layout == PCISPH_LAYOUT_FLOAT4 ? 16 : 4;
+        DeviceBlock& e = ctx->exports[field];
+        if (e.ensure(v.count * esz) != cudaSuccess) return fail(PCISPH_ERR_OOM, "device allocation of a field copy failed");
+        if (esz == 16) launch_gather4(static_cast<const float4*>(v.ptr), ctx->w_of_d, static_cast<float4*>(e.p), (uint32_t)v.count, ctx->stream());
+        else launch_gather1(static_cast<const float*>(v.ptr), ctx->w_of_d, static_cast<float*>(e.p), (uint32_t)v.count, ctx->stream());
+        ++ctx->host_launches;
+        CUDA_TRY(cudaGetLastError());
+        v.ptr = e.p;
+    }
     *ptr = v.ptr;
     if (count) *count = v.count;
     if (layout) *layout = v.layout;

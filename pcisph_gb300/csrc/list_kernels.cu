@@ -42,25 +42,25 @@ __device__ __forceinline__ void warp_atomic_max(unsigned* addr, unsigned v) {
     if ((int)(threadIdx.x & 31) == __ffs(peers) - 1) atomicMax(addr, m);
 }
 
-// Call f(j) for every listed neighbour, eight indices per two 16-byte loads (independent gathers in flight).
+// Call f(j) for the n listed neighbours of particle i in list order. col = nbr + i; entries are stride
+// apart. Eight entries are loaded before the first is used (eight independent gathers in flight); the
+// loads are streaming (evict-first), so the lists do not push the gathered particle data out of L2.
 template <class F>
-__device__ __forceinline__ void for_each_listed(const uint32_t* __restrict__ row, uint32_t n, F&& f) {
-    const uint4* r4 = reinterpret_cast<const uint4*>(row);
+__device__ __forceinline__ void for_each_listed(const uint32_t* __restrict__ col, uint32_t n, uint32_t stride,
+                                                F&& f) {
     uint32_t k = 0;
+    const size_t s = stride;
 #pragma unroll 1
     for (; k + 8 <= n; k += 8) {
-        const uint4 q = __ldg(&r4[k >> 2]);
-        const uint4 w = __ldg(&r4[(k >> 2) + 1]);
-        f(q.x);
-        f(q.y);
-        f(q.z);
-        f(q.w);
-        f(w.x);
-        f(w.y);
-        f(w.z);
-        f(w.w);
+        uint32_t j[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) j[u] = __ldcs(col + (size_t)u * s);
+        col += 8 * s;
+#pragma unroll
+        for (int u = 0; u < 8; ++u) f(j[u]);
     }
-    for (; k < n; ++k) f(__ldg(&row[k]));
+#pragma unroll 1
+    for (; k < n; ++k, col += s) f(__ldcs(col));
 }
 
 // After predicting x*_i (stored as xs): record the max displacement; a fast particle flags its bucket.
@@ -133,7 +133,8 @@ __global__ void __launch_bounds__(kBlock) k_density_list(PS ps, ListBuffers b) {
     float acc = 0.f;
     if (P.boundary_count)
         for_each_neighbour(b.b_cells, c, P, [&](uint32_t j) { acc += density_term(xi.x, xi.y, xi.z, __ldg(&b.b_pos[j]), P.h2); });
-    uint32_t* row = b.nbr + (size_t)i * P.list_cap;
+    uint32_t* col = b.nbr + i;
+    const size_t stride = b.nbr_stride;
     uint32_t n = 0;
     for_each_neighbour(b.cells, c, P, [&](uint32_t j) {
         const float4 o = __ldg(&b.pos[j]);
@@ -141,7 +142,7 @@ __global__ void __launch_bounds__(kBlock) k_density_list(PS ps, ListBuffers b) {
         const float r2 = dx * dx + dy * dy + dz * dz;
         acc += poly6(r2, P.h2);
         if (r2 <= P.list_r2) {
-            if (n < P.list_cap) row[n] = j;
+            if (n < P.list_cap) __stcs(col + n * stride, j);
             ++n;
         }
     });
@@ -161,7 +162,7 @@ __global__ void __launch_bounds__(kBlock) k_normal_list(PS ps, ListBuffers b) {
     float3 n = make_float3(0.f, 0.f, 0.f);
     const uint32_t cnt = b.nbr_count[i];
     auto f = [&](uint32_t j) { normal_term(xi.x, xi.y, xi.z, __ldg(&b.pr4[j]), P.h2, n); };
-    if (cnt <= P.list_cap) for_each_listed(b.nbr + (size_t)i * P.list_cap, cnt, f);
+    if (cnt <= P.list_cap) for_each_listed(b.nbr + i, cnt, b.nbr_stride, f);
     else for_each_neighbour(b.cells, cell_of(xi.x, xi.y, xi.z, P), P, f);
     const float scale = P.h * P.particle_mass * P.poly6_d1_norm;
     b.normal[i] = make_float4(n.x * scale, n.y * scale, n.z * scale, 0.f);
@@ -181,7 +182,7 @@ __global__ void __launch_bounds__(kBlock) k_force_list(PS ps, ListBuffers b) {
     auto f = [&](uint32_t j) {
         force_term(xi, vi, ni, __ldg(&b.pr4[j]), f3(__ldg(&b.vel[j])), f3(__ldg(&b.normal[j])), P, fa);
     };
-    if (cnt <= P.list_cap) for_each_listed(b.nbr + (size_t)i * P.list_cap, cnt, f);
+    if (cnt <= P.list_cap) for_each_listed(b.nbr + i, cnt, b.nbr_stride, f);
     else for_each_neighbour(b.cells, cell_of(xi.x, xi.y, xi.z, P), P, f);
     const float m = P.particle_mass;
     const float3 visc = fa.visc * (P.viscosity * m * P.visc_d2_norm);
@@ -217,7 +218,7 @@ __global__ void __launch_bounds__(kBlock) k_pressure_list(PS ps, ListBuffers b) 
             for_each_neighbour(b.b_cells, c, P, [&](uint32_t j) { acc += density_term(xp.x, xp.y, xp.z, __ldg(&b.b_pos[j]), P.h2); });
         auto f = [&](uint32_t j) { acc += density_term(xp.x, xp.y, xp.z, __ldg(&b.pred[j]), P.h2); };
         if (walk) for_each_neighbour(b.cells, c, P, f);
-        else for_each_listed(b.nbr + (size_t)i * P.list_cap, cnt, f);
+        else for_each_listed(b.nbr + i, cnt, b.nbr_stride, f);
         acc *= P.particle_mass * P.poly6_norm;
         if (!isfinite(acc)) atomicOr(&ctl->status, 2u);
         dv = acc - P.rest_density;
@@ -279,7 +280,7 @@ __global__ void __launch_bounds__(kBlock) k_pressure_force_list(PS ps, ListBuffe
     if (P.boundary_count)
         for_each_neighbour(b.b_cells, c, P, [&](uint32_t j) { pressure_force_term(xi, __ldg(&b.bpf[j]), P.h, P.h2, f); });
     auto body = [&](uint32_t j) { pressure_force_term(xi, __ldg(&b.pf4[j]), P.h, P.h2, f); };
-    if (cnt <= P.list_cap) for_each_listed(b.nbr + (size_t)i * P.list_cap, cnt, body);
+    if (cnt <= P.list_cap) for_each_listed(b.nbr + i, cnt, b.nbr_stride, body);
     else for_each_neighbour(b.cells, c, P, body);
     const float m = P.particle_mass;
     const float scale = -P.spiky_d1_norm * m * m;
@@ -310,8 +311,9 @@ __global__ void __launch_bounds__(kBlock) k_pressure_force_list(PS ps, ListBuffe
             }
         }
     }
-    b.state_pos[i] = f4(x, 0.f);
-    b.state_vel[i] = f4(v, 0.f);
+    const uint32_t o = b.out_index ? b.out_index[i] : i;  // working order -> sorted order
+    b.state_pos[o] = f4(x, 0.f);
+    b.state_vel[o] = f4(v, 0.f);
 }
 
 // Batch: close one corrective iteration per scene (one thread per scene) and set the graph's loop

@@ -233,7 +233,7 @@ class Fluid:
 
 
 def setup_scene(fluid, scene, walls=None, loop_mode=0, max_iters=None, min_iters=None, boundary_self_density=0,
-                kernel_variant=2):
+                kernel_variant=2, spatial_order=1):
     """Configure ``fluid`` for a scenes.Scene the way scene::load does (scenes.cpp:217-245)."""
     fluid.set_delta_t(scene.delta_t)
     fluid.set_rest_density(scene.rest_density)
@@ -248,7 +248,7 @@ def setup_scene(fluid, scene, walls=None, loop_mode=0, max_iters=None, min_iters
                       max_iterations=scene.max_iters if max_iters is None else max_iters,
                       walls=int(scene.walls if walls is None else walls), box_lo=scene.box_lo, box_hi=scene.box_hi,
                       restitution=scene.restitution, boundary_self_density=boundary_self_density,
-                      loop_mode=loop_mode, kernel_variant=kernel_variant)
+                      loop_mode=loop_mode, kernel_variant=kernel_variant, spatial_order=spatial_order)
     fluid.prepare()
     fluid.set_fluid_state(scene.fluid_pos, scene.fluid_vel)
     if scene.boundary_count:

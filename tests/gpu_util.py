@@ -34,7 +34,7 @@ def assert_close(name, got, want, scale=None, rtol=RTOL):
 
 
 def fluid_like(p, min_iters=3, max_iters=7, walls=False, box_lo=(0, 0, 0), box_hi=(0, 0, 0), restitution=0.5,
-               boundary_self_density=0, loop_mode=0, threshold=0.01, kernel_variant=2):
+               boundary_self_density=0, loop_mode=0, threshold=0.01, kernel_variant=2, spatial_order=1):
     """A context configured through the reference setters for params p (as scene::load does)."""
     f = Fluid(0)
     f.set_delta_t(p.delta_t)
@@ -48,7 +48,7 @@ def fluid_like(p, min_iters=3, max_iters=7, walls=False, box_lo=(0, 0, 0), box_h
     f.set_boundary_count(p.boundary_count)
     f.set_options(min_iterations=min_iters, max_iterations=max_iters, walls=int(walls), box_lo=box_lo,
                   box_hi=box_hi, restitution=restitution, boundary_self_density=boundary_self_density,
-                  loop_mode=loop_mode, kernel_variant=kernel_variant)
+                  loop_mode=loop_mode, kernel_variant=kernel_variant, spatial_order=spatial_order)
     f.prepare()
     return f
 

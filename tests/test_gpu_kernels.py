@@ -393,3 +393,53 @@ def test_list_sweeps_exact_with_fast_particles(oracle):
         e_list = rel_err(out[2][n], ref[n], scale)
         assert e_list <= max(2 * e_walk, 1e-6), (n, e_list, e_walk)
         assert rel_err(out[2][n], out[1][n], scale) <= 1e-5, n
+
+
+@pytest.mark.parametrize("case", ["dam", "drop"])
+def test_working_order_changes_no_result(case):
+    """The spatial working order (variant 2) moves whole buckets, keeping each bucket's sorted internal
+    order: every sum keeps its terms and their order, so results are identical to the sorted order, and
+    the exported fields come back in sorted order."""
+    from pcisph_gb300 import setup_scene
+    sc = scenes.small_dam(14, seed=5) if case == "dam" else scenes.batch_drop(4000, d=0.01, seed=6)
+    names = ("position", "velocity", "density", "pressure", "normal", "pressure_force", "other_force",
+             "predicted_position", "density_variation", "sorted_position", "sorted_velocity", "keys", "src",
+             "cell_offsets")
+    out = []
+    for so in (0, 1):
+        f = Fluid(0)
+        setup_scene(f, sc, kernel_variant=2, spatial_order=so)
+        f.step(8)
+        st = f.stats()
+        out.append(({n: f.get_field(n) for n in names}, (st.total_iterations, st.status_all, st.fast_particles)))
+        f.close()
+    for n in names:
+        np.testing.assert_array_equal(out[1][0][n], out[0][0][n], err_msg=n)
+    assert out[0][1] == out[1][1]
+
+
+def test_working_order_field_import_and_device_view():
+    """A field set in sorted order reads back unchanged; a device view of a working-order field is a
+    sorted-order copy."""
+    torch = _torch()
+    from pcisph_gb300 import setup_scene
+    sc = scenes.small_dam(9, seed=2)
+    f = Fluid(0)
+    setup_scene(f, sc, kernel_variant=2, spatial_order=1)
+    f.step(2)
+    rho = f.get_field("density")
+    want = np.arange(rho.size, dtype=np.float32) * 0.5 + 1.0
+    f.set_field("density", want)
+    np.testing.assert_array_equal(f.get_field("density"), want)
+    vec = np.random.default_rng(1).standard_normal((rho.size, 3)).astype(np.float32)
+    f.set_field("normal", vec)
+    np.testing.assert_array_equal(f.get_field("normal"), vec)
+
+    class View:  # zero-copy wrapper of the returned device pointer
+        def __init__(self, ptr, n):
+            self.__cuda_array_interface__ = {"shape": (n,), "typestr": "<f4", "data": (ptr, False), "version": 3}
+    ptr, n, lay = f.device_ptr("density")
+    f.sync()
+    view = torch.as_tensor(View(ptr, n), device="cuda")
+    np.testing.assert_array_equal(view.cpu().numpy(), want)
+    f.close()
