@@ -41,7 +41,7 @@ struct SceneSlot {
     bool removed;  // dropped at the next compaction
 };
 
-constexpr size_t kParticleBytes = 11 * 16 + 3 * 4 + 4 * 4 + 2 + kListCap * 4;  // the pool arrays of allocate()
+constexpr size_t kParticleBytes = 11 * 16 + 3 * 4 + 4 * 4 + 2 + (kListCap + kNearCap) * 4;  // allocate()'s arrays
 constexpr size_t kBucketBytesPerParticle = 5;  // (8 B table + 1 B flag) per bucket, ~N/2 buckets
 
 }  // namespace
@@ -53,7 +53,7 @@ struct pcisph_batch {
     DeviceBlock pool, tables;
     float4 *state_pos, *state_vel, *pos, *vel, *pr4, *normal, *f_other, *f_press, *pred, *pf4, *staging;
     float *rho, *press, *err;
-    uint32_t *keys, *ids, *nbr, *nbr_count;
+    uint32_t *keys, *ids, *nbr, *nbr_count, *near, *near_count;
     uint16_t* scene_of;
     uint2* cells;
     unsigned char* bucket_fast;
@@ -92,7 +92,8 @@ struct pcisph_batch {
     int allocate() {
         const size_t n = max_particles, nb = max_buckets, ns = max_scenes;
         const size_t bytes = 11 * align256(n * 16) + 3 * align256(n * 4) + 4 * align256(n * 4) + align256(n * 2) +
-                             align256(n * kListCap * 4) + align256(nb * 8) + align256(nb);
+                             align256(n * kListCap * 4) + align256(n * kNearCap * 4) + align256(nb * 8) +
+                             align256(nb);
         if (pool.ensure(bytes) != cudaSuccess)
             return report_error(PCISPH_ERR_OOM, "device allocation of the batch pool failed (" + std::to_string(bytes) + " bytes)");
         Carver c{static_cast<unsigned char*>(pool.p)};
@@ -113,9 +114,10 @@ struct pcisph_batch {
         keys = c.take<uint32_t>(n);
         ids = c.take<uint32_t>(n);
         nbr_count = c.take<uint32_t>(n);
-        c.take<uint32_t>(n);
+        near_count = c.take<uint32_t>(n);
         scene_of = c.take<uint16_t>(n);
         nbr = c.take<uint32_t>(n * kListCap);
+        near = c.take<uint32_t>(n * kNearCap);
         cells = c.take<uint2>(nb);
         bucket_fast = c.take<unsigned char>(nb);
         const size_t tbytes = align256(ns * sizeof(DevParams)) + align256(ns * sizeof(Control)) +
@@ -139,7 +141,8 @@ struct pcisph_batch {
     }
     ListBuffers list_buffers() const {
         return ListBuffers{pos, vel, pr4, normal, f_other, f_press, pred, pf4, state_pos, state_vel, rho, press, err,
-                           cells, cells, nullptr, nullptr, nbr, nbr_count, bucket_fast, n_particles, nullptr};
+                           cells, cells, nullptr, nullptr, nbr, nbr_count, near, near_count, bucket_fast,
+                           n_particles, nullptr};
     }
 
     uint32_t pool_end() const { return scenes.empty() ? 0u : scenes.back().offset + scenes.back().count; }

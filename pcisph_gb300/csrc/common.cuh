@@ -27,6 +27,8 @@ struct DevParams {
     uint32_t bucket_base;
     // neighbour lists (kernel_variant 2): capacity per particle, radius h (1 + skin) and its square
     uint32_t list_cap;
+    uint32_t near_cap;  // entries of the within-h list
+    float near_r2;      // within-h list radius^2: h^2 (1 + 1e-4), a margin far above rounding
     float list_r, list_r2, list_half_skin;
     // options
     int min_iters, max_iters, walls;
@@ -90,11 +92,11 @@ __device__ __forceinline__ uint32_t hash_key(uint32_t x, uint32_t y, uint32_t z,
     return mod_bk(v & 0x7FFFFFFFu, P);
 }
 
-// The 27 neighbour buckets in the reference's walk order (grid_utils.cl:68-69: x fastest).
-// body(j) is called for every particle index j in every bucket; no bucket is skipped or merged.
+// The ranges of the 27 neighbour buckets in the reference's walk order (grid_utils.cl:68-69: x fastest).
+// body(r) is called for every bucket's [r.x, r.y); no bucket is skipped or merged.
 template <class Body>
-__device__ __forceinline__ void for_each_neighbour(const uint2* __restrict__ cells, const Cell& c,
-                                                   const DevParams& P, Body&& body) {
+__device__ __forceinline__ void for_each_bucket(const uint2* __restrict__ cells, const Cell& c, const DevParams& P,
+                                                Body&& body) {
 #pragma unroll 1
     for (int dz = -1; dz <= 1; ++dz) {
         const uint32_t z = c.z + (uint32_t)dz;
@@ -107,11 +109,19 @@ __device__ __forceinline__ void for_each_neighbour(const uint2* __restrict__ cel
             for (int dx = -1; dx <= 1; ++dx) {
                 const uint32_t x = c.x + (uint32_t)dx;
                 const uint32_t v = (((x * 19349663u) ^ hyz) << 6) + (x & 63u) + lyz;
-                const uint2 r = __ldg(&cells[P.bucket_base + mod_bk(v & 0x7FFFFFFFu, P)]);
-                for (uint32_t j = r.x; j < r.y; ++j) body(j);
+                body(__ldg(&cells[P.bucket_base + mod_bk(v & 0x7FFFFFFFu, P)]));
             }
         }
     }
+}
+
+// body(j) for every particle index j of every neighbour bucket, in the walk order.
+template <class Body>
+__device__ __forceinline__ void for_each_neighbour(const uint2* __restrict__ cells, const Cell& c,
+                                                   const DevParams& P, Body&& body) {
+    for_each_bucket(cells, c, P, [&](uint2 r) {
+        for (uint32_t j = r.x; j < r.y; ++j) body(j);
+    });
 }
 
 // ---------------------------------------------------------------- vectors
@@ -123,6 +133,27 @@ __device__ __forceinline__ float3 operator*(float s, float3 a) { return make_flo
 __device__ __forceinline__ float3 operator/(float3 a, float s) { return make_float3(a.x / s, a.y / s, a.z / s); }
 __device__ __forceinline__ float dot3(float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 __device__ __forceinline__ float4 f4(float3 a, float w) { return make_float4(a.x, a.y, a.z, w); }
+
+// ------------------------------------------------------ fixed rounding
+// A sum of products leaves the compiler a choice of which product to fuse into an FMA, and the choice can
+// differ between kernels and template instantiations. These helpers fix the rounding, so every kernel
+// computes the same bits for the same inputs (one scene alone or in a batch, either particle order).
+
+// |d|^2 = dz^2 + (dy^2 + dx^2), each step rounded once
+__device__ __forceinline__ float dist2(float dx, float dy, float dz) {
+    return __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+}
+
+// F_other (pcisph.cl:161-172): (gravity + viscosity) + (cohesion + curvature), from the three neighbour
+// sums and their factors
+__device__ __forceinline__ float3 other_force(float m, float gravity, const float3& visc, float cv, const float3& coh,
+                                              float cc, const float3& curv, float cu) {
+    const float x = __fadd_rn(__fmul_rn(visc.x, cv), __fadd_rn(__fmul_rn(coh.x, cc), __fmul_rn(curv.x, cu)));
+    const float y = __fadd_rn(__fadd_rn(__fmul_rn(m, gravity), __fmul_rn(visc.y, cv)),
+                              __fadd_rn(__fmul_rn(coh.y, cc), __fmul_rn(curv.y, cu)));
+    const float z = __fadd_rn(__fmul_rn(visc.z, cv), __fadd_rn(__fmul_rn(coh.z, cc), __fmul_rn(curv.z, cu)));
+    return make_float3(x, y, z);
+}
 
 // ------------------------------------------------------ smoothing kernels (pcisph.cl:8-61)
 __device__ __forceinline__ float poly6(float r2, float h2) {

@@ -107,7 +107,8 @@ struct pcisph_ctx {
         const bool w = working_order();
         return ListBuffers{b.pos, b.vel, b.pr4, b.normal, b.f_other, b.f_press, b.pred, b.pf4, b.state_pos,
                            b.state_vel, b.rho, b.press, b.err, w ? cells_w : b.cells, b.b_cells, b.b_pos, b.bpf,
-                           b.nbr, b.nbr_count, b.bucket_fast, P.fluid_count, w ? d_of_w : nullptr};
+                           b.nbr, b.nbr_count, b.near, b.near_count, b.bucket_fast, P.fluid_count,
+                           w ? d_of_w : nullptr};
     }
 
     // Working-order buffers for n particles and bk buckets; the index maps start as the identity.
@@ -185,7 +186,8 @@ struct pcisph_ctx {
         if (!list_sweeps()) return PCISPH_OK;
         const size_t n = params.fluid_count;
         if (n >= (1u << 31)) return fail(PCISPH_ERR_INVALID_ARG, "kernel variant 2 takes fewer than 2^31 particles");
-        const size_t bytes = align256(n * P.list_cap * 4) + align256(n * 4) + align256(params.bucket_count);
+        const size_t bytes = align256(n * P.list_cap * 4) + align256(n * 4) + align256(n * P.near_cap * 4) +
+                             align256(n * 4) + align256(params.bucket_count);
         if (list_block.p && list_block.cap >= bytes && list_n == n) return PCISPH_OK;
         CUDA_TRY(cudaStreamSynchronize(stream()));
         if (list_block.ensure(bytes) != cudaSuccess)
@@ -193,6 +195,8 @@ struct pcisph_ctx {
         Carver c{static_cast<unsigned char*>(list_block.p)};
         b.nbr = c.take<uint32_t>(n * P.list_cap);
         b.nbr_count = c.take<uint32_t>(n);
+        b.near = c.take<uint32_t>(n * P.near_cap);
+        b.near_count = c.take<uint32_t>(n);
         b.bucket_fast = c.take<unsigned char>(params.bucket_count);
         list_n = n;
         graph_valid = false;

@@ -20,6 +20,7 @@ inline size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 
 inline constexpr float kPi = 3.14159265358979323846f;  // utils/constants.h:4
 inline constexpr uint32_t kListCap = 96;           // neighbour-list entries per particle (multiple of 4)
+inline constexpr uint32_t kNearCap = 64;           // within-h list entries per particle
 
 // Fluid.cpp:125-133
 inline uint32_t sort_bit_count_ref(uint32_t elements) {
@@ -148,6 +149,8 @@ inline void make_devparams(const pcisph_sim_params& p, int min_iters, int max_it
     magic_for(p.bucket_count, &d->bk_magic, &d->bk_shift);
     d->bucket_base = bucket_base;
     d->list_cap = kListCap;
+    d->near_cap = kNearCap;
+    d->near_r2 = p.kernel_radius2 * 1.0001f;
     d->list_r = p.kernel_radius * (1.f + list_skin);
     d->list_r2 = d->list_r * d->list_r;
     // half the skin, less a margin for the rounding of |x_i - x_j| and |x* - x| (relative 1e-6 of h)

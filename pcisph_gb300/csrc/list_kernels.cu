@@ -1,15 +1,17 @@
 // list_kernels.cu -- neighbour-list sweeps (kernel_variant 2), for one scene or a batch of scenes.
 //
 // The density sweep walks the reference's 27 buckets (grid_utils.cl:65-79) once per step and records,
-// per particle, every candidate j with |x_i - x_j| <= r_list = h (1 + skin), in walk order. The later
-// sweeps of the step (normal, force, and the pressure and pressure-force sweeps of every corrective
-// iteration) iterate that list instead of walking the buckets again: ~60 candidates per particle instead
-// of ~300. Because the list keeps the walk order and drops only pairs that contribute exactly zero, the
-// sums are the reference's sums in the reference's order.
+// per particle and in walk order, two lists: every candidate j with |x_i - x_j| <= r_list = h (1 + skin),
+// and the subset within h (plus a 1e-4 relative margin, far above rounding). The later sweeps of the step
+// iterate a list instead of walking the buckets again: the sweeps at the current positions (normal,
+// force, pressure force) the within-h list (~34 candidates), the pressure sweeps of the corrective
+// iterations the skin list (~65), instead of the walk's ~300. Because a list keeps the walk order and
+// drops only pairs that contribute exactly zero, the sums are the reference's sums in the reference's
+// order.
 //
 // Exactness conditions, checked on the device:
 //   - sweeps at the current positions x (normal, force, pressure force) need |x_i - x_j| <= h, always in
-//     the list;
+//     the within-h list;
 //   - the pressure sweep measures distances between predicted positions x*. A pair with
 //     |x*_i - x*_j| <= h has |x_i - x_j| <= h + |x*_i - x_i| + |x*_j - x_j|, so it is in both lists when
 //     both displacements are at most half the skin. A particle whose displacement exceeds that ("fast")
@@ -17,7 +19,8 @@
 //     whose 27 buckets include a flagged one walks the buckets instead of using its list: every pair with a
 //     fast particle j in i's walk (spatial neighbour or hash collision) is then summed by a walk. Flags
 //     last for the rest of the step;
-//   - a particle with more than list_cap candidates is marked (count > cap) and walks the buckets.
+//   - a particle with more than list_cap (near_cap) candidates is marked (count > cap) and walks the
+//     buckets in the sweeps that would use that list.
 // Boundary particles (B > 0, single scene) are summed by walking the boundary buckets.
 //
 // Parameter sources (list_kernels.cuh): OneScene passes one DevParams by value and the pressure kernel's
@@ -42,25 +45,63 @@ __device__ __forceinline__ void warp_atomic_max(unsigned* addr, unsigned v) {
     if ((int)(threadIdx.x & 31) == __ffs(peers) - 1) atomicMax(addr, m);
 }
 
-// Call f(j) for the n listed neighbours of particle i in list order. col = nbr + i; entries are stride
-// apart. Eight entries are loaded before the first is used (eight independent gathers in flight); the
-// loads are streaming (evict-first), so the lists do not push the gathered particle data out of L2.
+// List layout: entries k = 8c .. 8c+7 of particle i (chunk c) are 32 contiguous bytes at uint4 offset
+// 2 (c * stride + i); chunks are column-major over particles. A warp's 32 consecutive particles read
+// chunk c as 1 KB of contiguous memory, and the builder writes whole 32-byte sectors.
+__device__ __forceinline__ uint4* list_chunk(uint32_t* list, uint32_t i, uint32_t c, uint32_t stride) {
+    return reinterpret_cast<uint4*>(list) + 2 * ((size_t)c * stride + i);
+}
+
+// The builder stages each list's current chunk in shared memory, slot-major (buf[slot * kBlock + thread]:
+// conflict-free whatever slot each lane is at), and writes whole chunks.
+__device__ __forceinline__ void list_store_chunk(uint32_t* list, uint32_t i, uint32_t c, uint32_t stride,
+                                                 const uint32_t* buf) {
+    const uint32_t t = threadIdx.x;
+    uint4* p = list_chunk(list, i, c, stride);
+    __stcs(p, make_uint4(buf[t], buf[kBlock + t], buf[2 * kBlock + t], buf[3 * kBlock + t]));
+    __stcs(p + 1, make_uint4(buf[4 * kBlock + t], buf[5 * kBlock + t], buf[6 * kBlock + t], buf[7 * kBlock + t]));
+}
+
+// Append j as entry k of particle i's list.
+__device__ __forceinline__ void list_append(uint32_t* list, uint32_t i, uint32_t stride, uint32_t* buf, uint32_t k,
+                                            uint32_t j) {
+    buf[(k & 7u) * kBlock + threadIdx.x] = j;
+    if ((k & 7u) == 7u) list_store_chunk(list, i, k >> 3, stride, buf);
+}
+
+// Write the last, partial chunk of a list of n <= cap entries.
+__device__ __forceinline__ void list_finish(uint32_t* list, uint32_t i, uint32_t stride, const uint32_t* buf,
+                                            uint32_t n, uint32_t cap) {
+    if (n <= cap && (n & 7u)) list_store_chunk(list, i, n >> 3, stride, buf);
+}
+
+// Call f(j) for the n listed neighbours of particle i in list order. The next chunk's indices are loaded
+// while the current chunk's eight gathers are in flight, so the list stream and the gathers overlap. The
+// list loads are streaming (evict-first): the lists do not push the gathered particle data out of L2.
 template <class F>
-__device__ __forceinline__ void for_each_listed(const uint32_t* __restrict__ col, uint32_t n, uint32_t stride,
-                                                F&& f) {
-    uint32_t k = 0;
-    const size_t s = stride;
+__device__ __forceinline__ void for_each_listed(const uint32_t* __restrict__ list, uint32_t i, uint32_t n,
+                                                uint32_t stride, F&& f) {
+    const uint32_t chunks = (n + 7u) >> 3;
+    if (!chunks) return;
+    const uint4* p = list_chunk(const_cast<uint32_t*>(list), i, 0, stride);
+    const size_t step = 2 * (size_t)stride;
+    uint4 a = __ldcs(p), b = __ldcs(p + 1);
 #pragma unroll 1
-    for (; k + 8 <= n; k += 8) {
-        uint32_t j[8];
+    for (uint32_t c = 0; c < chunks; ++c) {
+        uint4 na = make_uint4(0u, 0u, 0u, 0u), nb = na;
+        if (c + 1 < chunks) {
+            p += step;
+            na = __ldcs(p);
+            nb = __ldcs(p + 1);
+        }
+        const uint32_t left = n - 8u * c;  // entries in this chunk: min(8, left)
+        const uint32_t e[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
 #pragma unroll
-        for (int u = 0; u < 8; ++u) j[u] = __ldcs(col + (size_t)u * s);
-        col += 8 * s;
-#pragma unroll
-        for (int u = 0; u < 8; ++u) f(j[u]);
+        for (int u = 0; u < 8; ++u)
+            if ((uint32_t)u < left) f(e[u]);
+        a = na;
+        b = nb;
     }
-#pragma unroll 1
-    for (; k < n; ++k, col += s) f(__ldcs(col));
 }
 
 // After predicting x*_i (stored as xs): record the max displacement; a fast particle flags its bucket.
@@ -68,7 +109,7 @@ __device__ __forceinline__ void note_displacement(const DevParams& P, Control* c
                                                   unsigned char* __restrict__ bucket_fast, const float4& xi,
                                                   const float4& xs) {
     const float dx = xs.x - xi.x, dy = xs.y - xi.y, dz = xs.z - xi.z;  // exact: xs and xi are close
-    const float disp = sqrtf(dx * dx + dy * dy + dz * dz);
+    const float disp = sqrtf(dist2(dx, dy, dz));
     warp_atomic_max(&ctl->max_disp_bits, __float_as_uint(disp));
     if (disp > P.list_half_skin) {
         atomicAdd(&ctl->fast_particles, 1ull);
@@ -133,20 +174,29 @@ __global__ void __launch_bounds__(kBlock) k_density_list(PS ps, ListBuffers b) {
     float acc = 0.f;
     if (P.boundary_count)
         for_each_neighbour(b.b_cells, c, P, [&](uint32_t j) { acc += density_term(xi.x, xi.y, xi.z, __ldg(&b.b_pos[j]), P.h2); });
-    uint32_t* col = b.nbr + i;
-    const size_t stride = b.nbr_stride;
-    uint32_t n = 0;
+    const uint32_t stride = b.nbr_stride;
+    uint32_t n = 0, nn = 0;
+    __shared__ uint32_t staged[2][8 * kBlock];  // current chunk of each thread's skin and within-h lists
+    uint32_t* fbuf = staged[0];
+    uint32_t* nbuf = staged[1];
     for_each_neighbour(b.cells, c, P, [&](uint32_t j) {
         const float4 o = __ldg(&b.pos[j]);
         const float dx = xi.x - o.x, dy = xi.y - o.y, dz = xi.z - o.z;
-        const float r2 = dx * dx + dy * dy + dz * dz;
+        const float r2 = dist2(dx, dy, dz);
         acc += poly6(r2, P.h2);
         if (r2 <= P.list_r2) {
-            if (n < P.list_cap) __stcs(col + n * stride, j);
+            if (n < P.list_cap) list_append(b.nbr, i, stride, fbuf, n, j);
             ++n;
+            if (r2 <= P.near_r2) {
+                if (nn < P.near_cap) list_append(b.near, i, stride, nbuf, nn, j);
+                ++nn;
+            }
         }
     });
-    b.nbr_count[i] = n;  // n > list_cap: this particle walks the buckets in the later sweeps
+    list_finish(b.nbr, i, stride, fbuf, n, P.list_cap);
+    list_finish(b.near, i, stride, nbuf, nn, P.near_cap);
+    b.nbr_count[i] = n;  // n > list_cap: this particle walks the buckets in the pressure sweeps
+    b.near_count[i] = nn;  // nn > near_cap: it walks them in the sweeps at the current positions
     acc *= P.particle_mass * P.poly6_norm;
     b.rho[i] = acc;
     b.pr4[i] = make_float4(xi.x, xi.y, xi.z, acc);
@@ -160,9 +210,9 @@ __global__ void __launch_bounds__(kBlock) k_normal_list(PS ps, ListBuffers b) {
     const DevParams& P = ps.params(i);
     const float4 xi = b.pr4[i];
     float3 n = make_float3(0.f, 0.f, 0.f);
-    const uint32_t cnt = b.nbr_count[i];
+    const uint32_t cnt = b.near_count[i];
     auto f = [&](uint32_t j) { normal_term(xi.x, xi.y, xi.z, __ldg(&b.pr4[j]), P.h2, n); };
-    if (cnt <= P.list_cap) for_each_listed(b.nbr + i, cnt, b.nbr_stride, f);
+    if (cnt <= P.near_cap) for_each_listed(b.near, i, cnt, b.nbr_stride, f);
     else for_each_neighbour(b.cells, cell_of(xi.x, xi.y, xi.z, P), P, f);
     const float scale = P.h * P.particle_mass * P.poly6_d1_norm;
     b.normal[i] = make_float4(n.x * scale, n.y * scale, n.z * scale, 0.f);
@@ -178,17 +228,15 @@ __global__ void __launch_bounds__(kBlock) k_force_list(PS ps, ListBuffers b) {
     const float3 vi = f3(b.vel[i]);
     const float3 ni = f3(b.normal[i]);
     ForceAccum fa{make_float3(0.f, 0.f, 0.f), make_float3(0.f, 0.f, 0.f), make_float3(0.f, 0.f, 0.f)};
-    const uint32_t cnt = b.nbr_count[i];
+    const uint32_t cnt = b.near_count[i];
     auto f = [&](uint32_t j) {
         force_term(xi, vi, ni, __ldg(&b.pr4[j]), f3(__ldg(&b.vel[j])), f3(__ldg(&b.normal[j])), P, fa);
     };
-    if (cnt <= P.list_cap) for_each_listed(b.nbr + i, cnt, b.nbr_stride, f);
+    if (cnt <= P.near_cap) for_each_listed(b.near, i, cnt, b.nbr_stride, f);
     else for_each_neighbour(b.cells, cell_of(xi.x, xi.y, xi.z, P), P, f);
     const float m = P.particle_mass;
-    const float3 visc = fa.visc * (P.viscosity * m * P.visc_d2_norm);
-    const float3 coh = fa.coh * (-P.st_coeff * m * m * P.st_norm);
-    const float3 curv = fa.curv * (-P.st_coeff * m);
-    const float3 fo = make_float3(0.f, m * P.gravity, 0.f) + visc + (coh + curv);
+    const float3 fo = other_force(m, P.gravity, fa.visc, P.viscosity * m * P.visc_d2_norm, fa.coh,
+                                  -P.st_coeff * m * m * P.st_norm, fa.curv, -P.st_coeff * m);
     b.f_other[i] = f4(fo, 0.f);
     b.press[i] = 0.f;
     const float3 v = vi + (fo / m) * P.dt;
@@ -218,7 +266,7 @@ __global__ void __launch_bounds__(kBlock) k_pressure_list(PS ps, ListBuffers b) 
             for_each_neighbour(b.b_cells, c, P, [&](uint32_t j) { acc += density_term(xp.x, xp.y, xp.z, __ldg(&b.b_pos[j]), P.h2); });
         auto f = [&](uint32_t j) { acc += density_term(xp.x, xp.y, xp.z, __ldg(&b.pred[j]), P.h2); };
         if (walk) for_each_neighbour(b.cells, c, P, f);
-        else for_each_listed(b.nbr + i, cnt, b.nbr_stride, f);
+        else for_each_listed(b.nbr, i, cnt, b.nbr_stride, f);
         acc *= P.particle_mass * P.poly6_norm;
         if (!isfinite(acc)) atomicOr(&ctl->status, 2u);
         dv = acc - P.rest_density;
@@ -274,13 +322,13 @@ __global__ void __launch_bounds__(kBlock) k_pressure_force_list(PS ps, ListBuffe
     Control* ctl = ps.control(i);
     const float4 xi = b.pf4[i];
     float3 f = make_float3(0.f, 0.f, 0.f);
-    const uint32_t cnt = b.nbr_count[i];
+    const uint32_t cnt = b.near_count[i];
     Cell c{0u, 0u, 0u};
-    if (cnt > P.list_cap || P.boundary_count) c = cell_of(xi.x, xi.y, xi.z, P);
+    if (cnt > P.near_cap || P.boundary_count) c = cell_of(xi.x, xi.y, xi.z, P);
     if (P.boundary_count)
         for_each_neighbour(b.b_cells, c, P, [&](uint32_t j) { pressure_force_term(xi, __ldg(&b.bpf[j]), P.h, P.h2, f); });
     auto body = [&](uint32_t j) { pressure_force_term(xi, __ldg(&b.pf4[j]), P.h, P.h2, f); };
-    if (cnt <= P.list_cap) for_each_listed(b.nbr + i, cnt, b.nbr_stride, body);
+    if (cnt <= P.near_cap) for_each_listed(b.near, i, cnt, b.nbr_stride, body);
     else for_each_neighbour(b.cells, c, P, body);
     const float m = P.particle_mass;
     const float scale = -P.spiky_d1_norm * m * m;

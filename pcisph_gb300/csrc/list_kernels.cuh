@@ -14,9 +14,12 @@ struct ListBuffers {
     const uint2* cells;
     const uint2* b_cells;
     const float4 *b_pos, *bpf;
-    uint32_t* nbr;               // list_cap entries per particle, column-major: entry k of particle i at
-                                 // nbr[k * nbr_stride + i] (a warp reads entry k of 32 particles in one line)
+    uint32_t* nbr;               // the skin list, list_cap entries per particle in chunks of 8: entries
+                                 // 8c..8c+7 of particle i at nbr[8 (c * nbr_stride + i)] (32 bytes)
     uint32_t* nbr_count;         // entries per particle; > list_cap: walk the buckets
+    uint32_t* near;              // the within-h list (pairs within h at the current positions), near_cap
+                                 // entries per particle, laid out like nbr
+    uint32_t* near_count;        // entries per particle; > near_cap: walk the buckets
     unsigned char* bucket_fast;  // per bucket of the cell table: holds a fast particle this step
     uint32_t nbr_stride;         // particles in the arrays (>= every index i)
     const uint32_t* out_index;   // integration writes particle i's state at out_index[i] (null: at i)

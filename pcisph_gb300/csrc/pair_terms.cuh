@@ -14,13 +14,13 @@ namespace pcisph {
 // poly6 for density and predicted density (pcisph.cl:8-16, :80, :242, :250)
 __device__ __forceinline__ float density_term(float xi, float yi, float zi, const float4& o, float h2) {
     const float dx = xi - o.x, dy = yi - o.y, dz = zi - o.z;
-    return poly6(dx * dx + dy * dy + dz * dz, h2);
+    return poly6(dist2(dx, dy, dz), h2);
 }
 
 // poly6 gradient over the neighbour's density (pcisph.cl:18-26, :107); o = (x_j, rho_j)
 __device__ __forceinline__ void normal_term(float xi, float yi, float zi, const float4& o, float h2, float3& n) {
     const float dx = xi - o.x, dy = yi - o.y, dz = zi - o.z;
-    const float r2 = dx * dx + dy * dy + dz * dz;
+    const float r2 = dist2(dx, dy, dz);
     if (r2 <= h2) {
         const float k = __fdividef((r2 - h2) * (r2 - h2), o.w);
         n.x += dx * k;
@@ -37,13 +37,13 @@ __device__ __forceinline__ void force_term(const float4& xi, const float3& vi, c
                                            const float3& vj, const float3& nj, const DevParams& P,
                                            ForceAccum& a) {
     const float dx = xi.x - o.x, dy = xi.y - o.y, dz = xi.z - o.z;
-    const float r2 = dx * dx + dy * dy + dz * dz;
+    const float r2 = dist2(dx, dy, dz);
     if (r2 <= P.h2) {
         const float inv_r = r2 > 0.f ? rsqrtf(r2) : 0.f;
-        const float dist = r2 * inv_r;
+        const float dist = __fmul_rn(r2, inv_r);  // rounded once: it has several uses
         const float rj = o.w;
         if (rj > 0.0001f) {
-            const float k = __fdividef(P.h - dist, rj);  // kernel_viscosity_d2 / rho_j
+            const float k = __fdividef(__fsub_rn(P.h, dist), rj);  // kernel_viscosity_d2 / rho_j
             a.visc.x += (vj.x - vi.x) * k;
             a.visc.y += (vj.y - vi.y) * k;
             a.visc.z += (vj.z - vi.z) * k;
@@ -64,10 +64,10 @@ __device__ __forceinline__ void force_term(const float4& xi, const float3& vi, c
 // spiky gradient times (p_i/rho_i^2 + p_j/rho_j^2) (pcisph.cl:28-37, :279-295); xi.w, o.w = p/rho^2
 __device__ __forceinline__ void pressure_force_term(const float4& xi, const float4& o, float h, float h2, float3& f) {
     const float dx = xi.x - o.x, dy = xi.y - o.y, dz = xi.z - o.z;
-    const float r2 = dx * dx + dy * dy + dz * dz;
+    const float r2 = dist2(dx, dy, dz);
     if (r2 <= h2 && r2 >= 1e-8f) {  // 1e-4 <= r <= h
         const float inv_r = rsqrtf(r2);
-        const float dr = h - r2 * inv_r;
+        const float dr = __fmaf_rn(-r2, inv_r, h);
         const float k = dr * dr * inv_r * (xi.w + o.w);
         f.x += dx * k;
         f.y += dy * k;

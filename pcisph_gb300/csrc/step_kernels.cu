@@ -111,13 +111,13 @@ __global__ void __launch_bounds__(kBlock) k_density(DevParams P, const uint2* __
         for_each_neighbour(b_cells, c, P, [&](uint32_t j) {
             const float4 o = __ldg(&b_pos[j]);
             const float dx = xi.x - o.x, dy = xi.y - o.y, dz = xi.z - o.z;
-            acc += poly6(dx * dx + dy * dy + dz * dz, h2);
+            acc += poly6(dist2(dx, dy, dz), h2);
         });
     }
     for_each_neighbour(cells, c, P, [&](uint32_t j) {
         const float4 o = __ldg(&pos[j]);
         const float dx = xi.x - o.x, dy = xi.y - o.y, dz = xi.z - o.z;
-        acc += poly6(dx * dx + dy * dy + dz * dz, h2);
+        acc += poly6(dist2(dx, dy, dz), h2);
     });
     acc *= P.particle_mass * P.poly6_norm;
     rho[i] = acc;
@@ -154,10 +154,8 @@ __global__ void __launch_bounds__(kBlock) k_force(DevParams P, const uint2* __re
         force_term(xi, vi, ni, __ldg(&pr4[j]), f3(__ldg(&vel[j])), f3(__ldg(&normal[j])), P, fa);
     });
     const float m = P.particle_mass;
-    const float3 visc = fa.visc * (P.viscosity * m * P.visc_d2_norm);
-    const float3 coh = fa.coh * (-P.st_coeff * m * m * P.st_norm);
-    const float3 curv = fa.curv * (-P.st_coeff * m);
-    const float3 fo = make_float3(0.f, m * P.gravity, 0.f) + visc + (coh + curv);
+    const float3 fo = other_force(m, P.gravity, fa.visc, P.viscosity * m * P.visc_d2_norm, fa.coh,
+                                  -P.st_coeff * m * m * P.st_norm, fa.curv, -P.st_coeff * m);
     f_other[i] = f4(fo, 0.f);
     press[i] = 0.f;
     const float3 a = fo / m;
@@ -178,7 +176,7 @@ __global__ void __launch_bounds__(kBlock) k_boundary_self_density(DevParams P, c
     for_each_neighbour(b_cells, c, P, [&](uint32_t j) {
         const float4 o = __ldg(&b_pos[j]);
         const float dx = xi.x - o.x, dy = xi.y - o.y, dz = xi.z - o.z;
-        acc += poly6(dx * dx + dy * dy + dz * dz, P.h2);
+        acc += poly6(dist2(dx, dy, dz), P.h2);
     });
     b_init[i] = acc;
 }
@@ -198,7 +196,7 @@ __global__ void __launch_bounds__(kBlock) k_boundary_pressure(DevParams P, const
     for_each_neighbour(cells, c, P, [&](uint32_t j) {
         const float4 o = __ldg(&pred[j]);
         const float dx = xb.x - o.x, dy = xb.y - o.y, dz = xb.z - o.z;
-        acc += poly6(dx * dx + dy * dy + dz * dz, P.h2);
+        acc += poly6(dist2(dx, dy, dz), P.h2);
     });
     acc *= P.particle_mass * P.poly6_norm;
     float dv = acc - P.rest_density;
@@ -229,13 +227,13 @@ __global__ void __launch_bounds__(kBlock) k_pressure(DevParams P, const uint2* _
             for_each_neighbour(b_cells, c, P, [&](uint32_t j) {
                 const float4 o = __ldg(&b_pos[j]);
                 const float dx = xp.x - o.x, dy = xp.y - o.y, dz = xp.z - o.z;
-                acc += poly6(dx * dx + dy * dy + dz * dz, h2);
+                acc += poly6(dist2(dx, dy, dz), h2);
             });
         }
         for_each_neighbour(cells, c, P, [&](uint32_t j) {
             const float4 o = __ldg(&pred[j]);
             const float dx = xp.x - o.x, dy = xp.y - o.y, dz = xp.z - o.z;
-            acc += poly6(dx * dx + dy * dy + dz * dz, h2);
+            acc += poly6(dist2(dx, dy, dz), h2);
         });
         acc *= P.particle_mass * P.poly6_norm;
         if (!isfinite(acc)) atomicOr(&ctl->status, 2u);

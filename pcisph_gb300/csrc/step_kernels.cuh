@@ -26,6 +26,8 @@ struct StepBuffers {
     uint32_t* groups;                // start of every bucket run (count in ctl->n_groups)
     uint32_t* nbr;                   // neighbour lists, list_cap entries per particle (kernel_variant 2)
     uint32_t* nbr_count;             // entries per particle; > list_cap means "walk the buckets"
+    uint32_t* near;                  // within-h lists, near_cap entries per particle
+    uint32_t* near_count;            // entries per particle; > near_cap means "walk the buckets"
     unsigned char* bucket_fast;      // per bucket: holds a particle predicted to move > skin / 2 (this step)
     // boundary
     float4 *b_pos, *bpf;

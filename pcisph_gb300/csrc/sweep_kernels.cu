@@ -51,7 +51,7 @@ struct OpDensity {
     __device__ void end(const DevParams&, const Result&) const {}
     __device__ __forceinline__ void pair(const DevParams& P, const Self& s, const Cand& o, Acc& a) const {
         const float dx = s.x - o.x, dy = s.y - o.y, dz = s.z - o.z;
-        a += poly6(dx * dx + dy * dy + dz * dz, P.h2);
+        a += poly6(dist2(dx, dy, dz), P.h2);
     }
     __device__ Result finish(const DevParams& P, uint32_t i, const Self& s, const Acc& a) const {
         const float r = a * (P.particle_mass * P.poly6_norm);
@@ -134,10 +134,8 @@ struct OpForce {
     }
     __device__ Result finish(const DevParams& P, uint32_t i, const Self& s, const Acc& a) const {
         const float m = P.particle_mass;
-        const float3 visc = a.visc * (P.viscosity * m * P.visc_d2_norm);
-        const float3 coh = a.coh * (-P.st_coeff * m * m * P.st_norm);
-        const float3 curv = a.curv * (-P.st_coeff * m);
-        const float3 fo = make_float3(0.f, m * P.gravity, 0.f) + visc + (coh + curv);
+        const float3 fo = other_force(m, P.gravity, a.visc, P.viscosity * m * P.visc_d2_norm, a.coh,
+                                      -P.st_coeff * m * m * P.st_norm, a.curv, -P.st_coeff * m);
         f_other[i] = f4(fo, 0.f);
         press[i] = 0.f;
         const float3 v = s.v + (fo / m) * P.dt;
@@ -180,7 +178,7 @@ struct OpPressure {
     __device__ void begin(const DevParams&) const {}
     __device__ __forceinline__ void pair(const DevParams& P, const Self& s, const Cand& o, Acc& a) const {
         const float dx = s.xp.x - o.x, dy = s.xp.y - o.y, dz = s.xp.z - o.z;
-        a += poly6(dx * dx + dy * dy + dz * dz, P.h2);
+        a += poly6(dist2(dx, dy, dz), P.h2);
     }
     __device__ Result finish(const DevParams& P, uint32_t i, const Self& s, const Acc& a) const {
         const float rs = a * (P.particle_mass * P.poly6_norm);
