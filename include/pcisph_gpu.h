@@ -221,6 +221,16 @@ PCISPH_API int pcisph_run_stage(pcisph_ctx* ctx, int stage, int arg);
 /* Kernels launched by this context since creation (for launch accounting). */
 PCISPH_API uint64_t pcisph_kernel_launches(const pcisph_ctx* ctx);
 
+/* Checkpoints. A snapshot is a self-describing host buffer: a header (magic "PCSN", format version, the
+ * sizes of the parameter and option records, particle counts, threshold, steps taken), the parameter
+ * setters' values, the options, then the fluid positions and velocities (float4 per particle, sorted
+ * order of the last step) and the boundary positions as set (float4). pcisph_snapshot synchronises the
+ * context's stream. pcisph_restore sets the parameters and options, re-derives them and loads the state,
+ * so the next update continues exactly where the snapshot was taken. No counterpart in the reference. */
+PCISPH_API int pcisph_snapshot_size(pcisph_ctx* ctx, size_t* bytes);
+PCISPH_API int pcisph_snapshot(pcisph_ctx* ctx, void* dst, size_t dst_bytes);
+PCISPH_API int pcisph_restore(pcisph_ctx* ctx, const void* src, size_t src_bytes);
+
 /* Per-kernel CUDA-event timing of the host-driven path (loop_mode 1 timing is used while enabled). */
 typedef struct pcisph_kernel_time {
     char name[32];
@@ -285,6 +295,28 @@ PCISPH_API int pcisph_batch_set_state(pcisph_batch* batch, int32_t scene_id, con
 PCISPH_API int pcisph_batch_get_field(pcisph_batch* batch, int32_t scene_id, int field, void* dst,
                                       size_t dst_bytes, int layout, int memory);
 PCISPH_API uint64_t pcisph_batch_kernel_launches(const pcisph_batch* batch);
+
+/* ------------------------------------------------------------ rendering */
+/* Headless replacement of the reference's OpenGL particle rendering (vis/fluid_rendering.cpp:65-103 with
+ * data/shaders/simple_particle.vert and .frag): spheres of the particle radius coloured by density
+ * (blue at 0.95 rho0, purple at rho0, orange at 1.05 rho0), lit from +y with 0.2 ambient, darkened with
+ * view depth from 5 to 20. The reference's camera is eye = d (sin a, 0.2, cos a), target 0, up +y, 60
+ * degrees horizontal field of view (main.cpp:174-179). Output: RGB8, row 0 at the top. */
+typedef struct pcisph_camera {
+    float eye[3];
+    float target[3];
+    float up[3];
+    float fov_x_degrees;
+} pcisph_camera;
+/* Device pointers: pos4 (n float4), density (n floats, or NULL: all at rest density), zbuffer (width *
+ * height * 8 bytes of scratch), rgb (width * height * 3 bytes). Stream-ordered on `stream`. */
+PCISPH_API int pcisph_render(const float* pos4, const float* density, uint32_t n, float particle_radius,
+                             float rest_density, const pcisph_camera* cam, int width, int height, void* zbuffer,
+                             size_t zbuffer_bytes, uint8_t* rgb, void* stream);
+/* The context's fluid (positions and densities of the last step) into a host RGB8 image of width * height
+ * * 3 bytes (synchronises). */
+PCISPH_API int pcisph_render_fluid(pcisph_ctx* ctx, const pcisph_camera* cam, int width, int height, uint8_t* rgb,
+                                   size_t rgb_bytes);
 
 /* --------------------------------------------------- standalone kernels */
 /* sort_utils.cl:12-23: key = hash(floor(pos / cell_size)) % bucket_count, id = index. Device pointers. */

@@ -41,8 +41,10 @@ def build_reference(force=False):
     if not reference_available():
         return REF_SO if os.path.exists(REF_SO) else None
     deps = [os.path.join(HERE, "build_ref.sh"), os.path.join(HERE, "ref_shim", "cl_shim.h"),
-            os.path.join(HERE, "ref_shim", "ref_driver.cpp")]
-    if force or _stale(REF_SO, deps):
+            os.path.join(HERE, "ref_shim", "ref_driver.cpp"), os.path.join(HERE, "ref_shim", "scene_shim.cpp"),
+            os.path.join(HERE, "ref_shim", "scene_entry.cpp")]
+    scene_so = os.path.join(os.path.dirname(REF_SO), "libpcisph_ref_scene.so")
+    if force or _stale(REF_SO, deps) or _stale(scene_so, deps):
         subprocess.run(["bash", os.path.join(HERE, "build_ref.sh"), REFERENCE_ROOT], check=True,
                        stdout=subprocess.DEVNULL)
     return REF_SO

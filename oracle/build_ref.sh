@@ -44,3 +44,17 @@ rewrite() { sed -E 's/\((float3|uint2)\)[[:space:]]*\(/\1(/g' "$1"; }
         -o "$OUT/libpcisph_ref.so.tmp" -
 mv "$OUT/libpcisph_ref.so.tmp" "$OUT/libpcisph_ref.so"
 echo "built $OUT/libpcisph_ref.so"
+
+# The reference's scene loader: scenes.cpp from "namespace scene {" up to (not including) load_xraw, which
+# needs OpenGL; utils::read_file comes from ref_shim/scene_shim.cpp.
+{
+    echo "#line 1 \"oracle/ref_shim/scene_shim.cpp\""
+    cat "$HERE/ref_shim/scene_shim.cpp"
+    echo "#line 11 \"PCISPH/src/scenes.cpp\""
+    sed -n '/^namespace scene {/,/void load_xraw(const std::string& path/p' "$SRC/src/scenes.cpp" | sed '$d'
+    echo "}  // namespace scene"
+    echo "#line 1 \"oracle/ref_shim/scene_entry.cpp\""
+    cat "$HERE/ref_shim/scene_entry.cpp"
+} | g++ -x c++ -std=c++17 -O2 -ffp-contract=off -w -fPIC -shared -o "$OUT/libpcisph_ref_scene.so.tmp" -
+mv "$OUT/libpcisph_ref_scene.so.tmp" "$OUT/libpcisph_ref_scene.so"
+echo "built $OUT/libpcisph_ref_scene.so"

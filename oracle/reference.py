@@ -6,6 +6,7 @@ present, to check the oracle directly. Each ``ref_*`` symbol runs one reference
 kernel as an NDRange (see ``ref_shim/ref_driver.cpp``).
 """
 import ctypes as C
+import os
 
 import numpy as np
 
@@ -142,3 +143,26 @@ class Reference:
                                _u(s["f_keys"]), _u(s["f_src"]), _f(tmp["f_pos_tmp"]), _f(tmp["f_vel_tmp"]),
                                _f(s["f_err"]), C.byref(me))
         return it, me.value
+
+
+def load_xraw_reference(path, particles_per_dimension, scaling):
+    """The reference's own scene loader (scenes.cpp:76-149, compiled by build_ref.sh into
+    libpcisph_ref_scene.so): (fluid, boundary, visible cubes) positions, each (n, 3) float32."""
+    lib_path = os.path.join(os.path.dirname(build_reference() or ""), "libpcisph_ref_scene.so")
+    L = C.CDLL(lib_path)
+    fp, ul = C.POINTER(C.c_float), C.c_ulong
+    L.ref_load_xraw.argtypes = [C.c_char_p, C.c_uint, C.c_float, C.POINTER(fp), C.POINTER(ul), C.POINTER(fp),
+                                C.POINTER(ul), C.POINTER(fp), C.POINTER(ul)]
+    L.ref_free.argtypes = [C.c_void_p]
+    ptrs, counts = [fp() for _ in range(3)], [ul() for _ in range(3)]
+    rc = L.ref_load_xraw(str(path).encode(), int(particles_per_dimension), C.c_float(scaling),
+                         C.byref(ptrs[0]), C.byref(counts[0]), C.byref(ptrs[1]), C.byref(counts[1]),
+                         C.byref(ptrs[2]), C.byref(counts[2]))
+    if rc:
+        raise FileNotFoundError(path)
+    out = []
+    for ptr, n in zip(ptrs, counts):
+        out.append(np.ctypeslib.as_array(ptr, (n.value * 3,)).reshape(-1, 3).copy() if n.value
+                   else np.zeros((0, 3), np.float32))
+        L.ref_free(ptr)
+    return tuple(out)

@@ -68,6 +68,11 @@ class SceneDesc(C.Structure):
                 ("box_lo", C.c_float * 3), ("box_hi", C.c_float * 3), ("restitution", C.c_float)]
 
 
+class Camera(C.Structure):
+    _fields_ = [("eye", C.c_float * 3), ("target", C.c_float * 3), ("up", C.c_float * 3),
+                ("fov_x_degrees", C.c_float)]
+
+
 class KernelTime(C.Structure):
     _fields_ = [("name", C.c_char * 32), ("launches", C.c_uint64), ("total_ms", C.c_double)]
 
@@ -132,6 +137,12 @@ def load():
         "pcisph_set_field": ([vp, i32, vp, sz, i32, i32], i32),
         "pcisph_field_device_ptr": ([vp, i32, C.POINTER(vp), C.POINTER(sz), C.POINTER(i32)], i32),
         "pcisph_run_stage": ([vp, i32, i32], i32),
+        "pcisph_render": ([vp, vp, C.c_uint32, C.c_float, C.c_float, C.POINTER(Camera), i32, i32, vp, sz, vp, vp],
+                          i32),
+        "pcisph_render_fluid": ([vp, C.POINTER(Camera), i32, i32, vp, sz], i32),
+        "pcisph_snapshot_size": ([vp, C.POINTER(sz)], i32),
+        "pcisph_snapshot": ([vp, vp, sz], i32),
+        "pcisph_restore": ([vp, vp, sz], i32),
         "pcisph_kernel_launches": ([vp], C.c_uint64),
         "pcisph_profile_enable": ([vp, i32], i32),
         "pcisph_profile_read": ([vp, C.POINTER(KernelTime), i32, C.POINTER(i32)], i32),

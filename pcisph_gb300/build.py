@@ -14,7 +14,7 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libpcisph_gb300.so")
-SOURCES = ["context.cu", "batch.cu", "step_kernels.cu", "sweep_kernels.cu", "list_kernels.cu", "spatial_order.cu", "radix_sort.cu",
+SOURCES = ["context.cu", "batch.cu", "step_kernels.cu", "sweep_kernels.cu", "list_kernels.cu", "spatial_order.cu", "render.cu", "radix_sort.cu",
            "radix_sort_noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2,-fvisibility=hidden",

@@ -86,6 +86,7 @@ struct pcisph_ctx {
     RadixSorter bucket_sorter;
     size_t order_n = 0, order_bk = 0;
     std::map<int, DeviceBlock> exports;  // sorted-order copies handed out by pcisph_field_device_ptr
+    DeviceBlock render_block;            // depth buffer and image of pcisph_render_fluid
     StepBuffers b{};
     float4* b_pos_in = nullptr;
     uint32_t *f_keys = nullptr, *f_ids = nullptr, *b_keys = nullptr, *b_ids = nullptr;
@@ -797,6 +798,7 @@ struct pcisph_ctx {
         order_block.release();
         bucket_sort_block.release();
         for (auto& kv : exports) kv.second.release();
+        render_block.release();
         if (host_ctl) cudaFreeHost(host_ctl);
         if (capture_stream) cudaStreamDestroy(capture_stream);
         if (own_stream) cudaStreamDestroy(own_stream);
@@ -1075,6 +1077,132 @@ int pcisph_field_device_ptr(pcisph_ctx* ctx, int field, void** ptr, size_t* coun
     *ptr = v.ptr;
     if (count) *count = v.count;
     if (layout) *layout = v.layout;
+    return PCISPH_OK;
+}
+
+namespace {
+struct SnapshotHeader {
+    char magic[4];           // "PCSN"
+    uint32_t version;        // 1
+    uint32_t params_bytes;   // sizeof(pcisph_sim_params)
+    uint32_t options_bytes;  // sizeof(pcisph_options)
+    uint32_t fluid_count, boundary_count;
+    float threshold;
+    uint32_t reserved;
+    uint64_t steps;
+};
+size_t snapshot_bytes(uint32_t n, uint32_t b) {
+    return sizeof(SnapshotHeader) + sizeof(pcisph_sim_params) + sizeof(pcisph_options) + (size_t)n * 32 +
+           (size_t)b * 16;
+}
+}  // namespace
+
+int pcisph_snapshot_size(pcisph_ctx* ctx, size_t* bytes) {
+    if (!ctx || !bytes) return fail(PCISPH_ERR_INVALID_ARG, "NULL argument");
+    *bytes = snapshot_bytes(ctx->params.fluid_count, ctx->params.boundary_count);
+    return PCISPH_OK;
+}
+
+int pcisph_snapshot(pcisph_ctx* ctx, void* dst, size_t dst_bytes) {
+    if (!ctx || !dst) return fail(PCISPH_ERR_INVALID_ARG, "NULL argument");
+    const uint32_t N = ctx->params.fluid_count, B = ctx->params.boundary_count;
+    const size_t need = snapshot_bytes(N, B);
+    if (dst_bytes < need) return fail(PCISPH_ERR_INVALID_ARG, "snapshot buffer too small: need " + std::to_string(need));
+    if (ctx->fluid_loaded != N || (B && ctx->boundary_loaded != B))
+        return fail(PCISPH_ERR_NOT_READY, "no state to snapshot (set the fluid and boundary state first)");
+    DeviceGuard g(ctx->device);
+    CUDA_TRY(cudaStreamSynchronize(ctx->stream()));
+    Control c{};
+    CUDA_TRY(cudaMemcpy(&c, ctx->ctl, sizeof(Control), cudaMemcpyDeviceToHost));
+    unsigned char* p = static_cast<unsigned char*>(dst);
+    SnapshotHeader h{{'P', 'C', 'S', 'N'}, 1u, (uint32_t)sizeof(pcisph_sim_params), (uint32_t)sizeof(pcisph_options),
+                     N, B, ctx->threshold, 0u, c.steps};
+    std::memcpy(p, &h, sizeof h);
+    p += sizeof h;
+    std::memcpy(p, &ctx->params, sizeof(pcisph_sim_params));
+    p += sizeof(pcisph_sim_params);
+    std::memcpy(p, &ctx->opts, sizeof(pcisph_options));
+    p += sizeof(pcisph_options);
+    if (N) {
+        CUDA_TRY(cudaMemcpy(p, ctx->b.state_pos, (size_t)N * 16, cudaMemcpyDeviceToHost));
+        CUDA_TRY(cudaMemcpy(p + (size_t)N * 16, ctx->b.state_vel, (size_t)N * 16, cudaMemcpyDeviceToHost));
+        p += (size_t)N * 32;
+    }
+    if (B) CUDA_TRY(cudaMemcpy(p, ctx->b_pos_in, (size_t)B * 16, cudaMemcpyDeviceToHost));
+    return PCISPH_OK;
+}
+
+int pcisph_restore(pcisph_ctx* ctx, const void* src, size_t src_bytes) {
+    if (!ctx || !src) return fail(PCISPH_ERR_INVALID_ARG, "NULL argument");
+    SnapshotHeader h;
+    if (src_bytes < sizeof h) return fail(PCISPH_ERR_INVALID_ARG, "snapshot truncated");
+    std::memcpy(&h, src, sizeof h);
+    if (std::memcmp(h.magic, "PCSN", 4) != 0 || h.version != 1u || h.params_bytes != sizeof(pcisph_sim_params) ||
+        h.options_bytes != sizeof(pcisph_options))
+        return fail(PCISPH_ERR_INVALID_ARG, "not a snapshot of this library version");
+    if (src_bytes < snapshot_bytes(h.fluid_count, h.boundary_count))
+        return fail(PCISPH_ERR_INVALID_ARG, "snapshot truncated");
+    const unsigned char* p = static_cast<const unsigned char*>(src) + sizeof h;
+    pcisph_sim_params sp;
+    pcisph_options o;
+    std::memcpy(&sp, p, sizeof sp);
+    p += sizeof sp;
+    std::memcpy(&o, p, sizeof o);
+    p += sizeof o;
+    if (sp.fluid_count != h.fluid_count || sp.boundary_count != h.boundary_count)
+        return fail(PCISPH_ERR_INVALID_ARG, "snapshot counts disagree with its parameters");
+    int rc = pcisph_set_options(ctx, &o);
+    if (rc) return rc;
+    // the nine setters (Fluid.h:21-29), then the derivation (which zeroes velocities), then the state
+    ctx->params.fluid_count = sp.fluid_count;
+    ctx->params.boundary_count = sp.boundary_count;
+    ctx->params.delta_t = sp.delta_t;
+    ctx->params.rest_density = sp.rest_density;
+    ctx->params.particle_radius = sp.particle_radius;
+    ctx->params.gravity = sp.gravity;
+    ctx->params.viscosity_constant = sp.viscosity_constant;
+    ctx->params.surface_tension_coefficient = sp.surface_tension_coefficient;
+    ctx->params_changed = true;
+    rc = pcisph_set_density_variation_threshold(ctx, h.threshold);
+    if (!rc) rc = pcisph_prepare(ctx);
+    if (rc) return rc;
+    const float* f = reinterpret_cast<const float*>(p);
+    rc = pcisph_set_fluid_state(ctx, f, f + (size_t)h.fluid_count * 4, h.fluid_count, PCISPH_LAYOUT_FLOAT4,
+                                PCISPH_MEM_HOST);
+    if (rc) return rc;
+    if (h.boundary_count)
+        rc = pcisph_set_boundary_state(ctx, f + (size_t)h.fluid_count * 8, h.boundary_count, PCISPH_LAYOUT_FLOAT4,
+                                       PCISPH_MEM_HOST);
+    return rc;
+}
+
+int pcisph_render_fluid(pcisph_ctx* ctx, const pcisph_camera* cam, int width, int height, uint8_t* rgb,
+                        size_t rgb_bytes) {
+    if (!ctx || !cam || !rgb) return fail(PCISPH_ERR_INVALID_ARG, "NULL argument");
+    if (width <= 0 || height <= 0 || width > 16384 || height > 16384)
+        return fail(PCISPH_ERR_INVALID_ARG, "image size must be in 1..16384");
+    const size_t pixels = (size_t)width * height;
+    if (rgb_bytes < pixels * 3) return fail(PCISPH_ERR_INVALID_ARG, "rgb buffer needs width * height * 3 bytes");
+    const uint32_t N = ctx->params.fluid_count;
+    if (N && ctx->fluid_loaded != N) return fail(PCISPH_ERR_NOT_READY, "no fluid state to render");
+    DeviceGuard g(ctx->device);
+    void* density = nullptr;
+    if (N && ctx->b.rho && ctx->steps_launched) {  // densities of the last step, in the state's order
+        size_t cnt = 0;
+        int rc = pcisph_field_device_ptr(ctx, PCISPH_FIELD_DENSITY, &density, &cnt, nullptr);
+        if (rc) return rc;
+    }
+    DeviceBlock& img = ctx->render_block;
+    const size_t zbytes = align256(pixels * 8);
+    if (img.ensure(zbytes + pixels * 3) != cudaSuccess) return fail(PCISPH_ERR_OOM, "device allocation of the image failed");
+    uint8_t* d_rgb = static_cast<uint8_t*>(img.p) + zbytes;
+    int rc = pcisph_render(reinterpret_cast<const float*>(ctx->b.state_pos), static_cast<const float*>(density), N,
+                           ctx->params.particle_radius, ctx->params.rest_density, cam, width, height, img.p, zbytes,
+                           d_rgb, ctx->stream());
+    if (rc) return rc;
+    ctx->host_launches += 2;
+    CUDA_TRY(cudaMemcpyAsync(rgb, d_rgb, pixels * 3, cudaMemcpyDeviceToHost, ctx->stream()));
+    CUDA_TRY(cudaStreamSynchronize(ctx->stream()));
     return PCISPH_OK;
 }
 

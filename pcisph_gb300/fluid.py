@@ -156,6 +156,29 @@ class Fluid:
     def reset_stats(self):
         check(self._L.pcisph_reset_stats(self._h))
 
+    # -- checkpoints ----------------------------------------------------------
+    def snapshot(self):
+        """The context's parameters, options and state as bytes (pcisph_snapshot)."""
+        n = C.c_size_t()
+        check(self._L.pcisph_snapshot_size(self._h, C.byref(n)))
+        buf = C.create_string_buffer(n.value)
+        check(self._L.pcisph_snapshot(self._h, buf, n.value))
+        return buf.raw
+
+    def restore(self, data):
+        """Continue from a snapshot (pcisph_restore)."""
+        buf = C.create_string_buffer(bytes(data), len(data))
+        check(self._L.pcisph_restore(self._h, buf, len(data)))
+
+    def save(self, path):
+        """Write a checkpoint file (the snapshot bytes)."""
+        with open(path, "wb") as f:
+            f.write(self.snapshot())
+
+    def load(self, path):
+        with open(path, "rb") as f:
+            self.restore(f.read())
+
     def run_stage(self, stage, arg=0):
         check(self._L.pcisph_run_stage(self._h, STAGES[stage], int(arg)))
 

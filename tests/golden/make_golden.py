@@ -7,7 +7,7 @@ sequence and stores inputs and outputs of every stage. It needs the reference
 sources, so it runs only where they exist; the .npz files it writes are
 committed and are what the tests read.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [fixture names]   (default: all)
 """
 import os
 import sys
@@ -151,21 +151,72 @@ def gen_scene(R, name, sc, b_pos0, viscosity, surface_tension, gravity, rest_den
     print(name, "N", N, "B", B, "iters", [int(g[f"step{k}_iters"]) for k in range(nsteps)])
 
 
-def main():
+XRAW_SCENES = ("simple_drop", "dambreak", "cube_splash")
+
+
+def gen_xraw():
+    """The reference's three voxel scenes (PCISPH/data/scenes/*.xraw) as voxel grids, with what the
+    reference's own loader (scenes.cpp:76-149) makes of them at its particles-per-voxel settings
+    (scenes.cpp:229-236) and at 3: particle counts and SHA-256 of the float32 position arrays."""
+    import hashlib
+    import struct
+
+    from oracle.build import REFERENCE_ROOT
+    from oracle.reference import load_xraw_reference
+    from pcisph_gb300.xraw import REFERENCE_SCENES
+    out = {}
+    for name in XRAW_SCENES:
+        path = os.path.join(REFERENCE_ROOT, "PCISPH", "data", "scenes", name + ".xraw")
+        data = open(path, "rb").read()
+        sx, sy, sz, _ = struct.unpack_from("<4I", data, 8)
+        out[f"{name}_size"] = np.array([sx, sy, sz], np.uint32)
+        out[f"{name}_voxels"] = np.frombuffer(data, np.uint8, count=sx * sy * sz, offset=24).reshape(sz, sy, sx).copy()
+        for ppd in sorted({REFERENCE_SCENES[name]["particles_per_dimension"], 3}):
+            arrays = load_xraw_reference(path, ppd, 0.7)
+            for kind, a in zip(("fluid", "boundary", "cubes"), arrays):
+                out[f"{name}_ppd{ppd}_{kind}_count"] = np.int64(a.shape[0])
+                out[f"{name}_ppd{ppd}_{kind}_sha256"] = np.array(hashlib.sha256(a.tobytes()).hexdigest())
+        print(name, (sx, sy, sz), {k: int(v) for k, v in out.items() if k.startswith(name) and k.endswith("count")})
+    np.savez_compressed(os.path.join(OUT, "xraw_scenes.npz"), **out)
+
+
+def gen_dambreak_steps(R):
+    """The reference's dambreak scene (decoded by its own loader at 3 particles per voxel edge, boundary
+    particles included) stepped by the reference's own kernels with its settings (scenes.cpp:219-224)."""
+    from oracle.build import REFERENCE_ROOT
+    from oracle.reference import load_xraw_reference
+    path = os.path.join(REFERENCE_ROOT, "PCISPH", "data", "scenes", "dambreak.xraw")
+    fluid, boundary, _ = load_xraw_reference(path, 3, 0.7)
+    sc = scenes.Scene("dambreak_ppd3", fluid, 0.7 / 3, 0.002, walls=False)
+    gen_scene(R, "step_dambreak", sc, boundary, 8e-5, 1.0, -9.81, 999.972, 0.0, 3, seed=9)
+
+
+GENERATORS = {
+    "params": lambda R: gen_params(R), "hash": lambda R: gen_hash(R), "sort": lambda R: gen_sort(R),
+    "step_boundary": None, "step_fluid": None, "xraw_scenes": lambda R: gen_xraw(),
+    "step_dambreak": lambda R: gen_dambreak_steps(R),
+}
+
+
+def main(names):
     R = Reference()
-    gen_params(R)
-    gen_hash(R)
-    gen_sort(R)
-    # reference-style scene: fluid block in a box lined with boundary particles (reference defaults,
-    # scenes.cpp:219-224, with the dambreak resolution ppd = 18 at scaling 0.7)
-    d = 0.7 / 18
-    sc = scenes.dam_break(9, seed=5, extent=9 * d, box=(0, 0, 0), delta_t=0.002)
-    b_pos0 = scenes.boundary_box((0, 0, 0), (12 * d, 12 * d, 12 * d), d, layers=1)
-    gen_scene(R, "step_boundary", sc, b_pos0, 8e-5, 1.0, -9.81, 999.972, 0.05, 2, seed=6)
-    # fluid only, config-0 physics (no walls in the reference)
-    sc = scenes.small_dam(10, seed=7)
-    gen_scene(R, "step_fluid", sc, np.zeros((0, 3), np.float32), 1.6e-6, 0.5, -9.81, 1000.0, 0.05, 2, seed=8)
+    names = names or list(GENERATORS)
+    for name in names:
+        if name == "step_boundary":
+            # reference-style scene: fluid block in a box lined with boundary particles (reference defaults,
+            # scenes.cpp:219-224, with the dambreak resolution ppd = 18 at scaling 0.7)
+            d = 0.7 / 18
+            sc = scenes.dam_break(9, seed=5, extent=9 * d, box=(0, 0, 0), delta_t=0.002)
+            b_pos0 = scenes.boundary_box((0, 0, 0), (12 * d, 12 * d, 12 * d), d, layers=1)
+            gen_scene(R, "step_boundary", sc, b_pos0, 8e-5, 1.0, -9.81, 999.972, 0.05, 2, seed=6)
+        elif name == "step_fluid":
+            # fluid only, config-0 physics (no walls in the reference)
+            sc = scenes.small_dam(10, seed=7)
+            gen_scene(R, "step_fluid", sc, np.zeros((0, 3), np.float32), 1.6e-6, 0.5, -9.81, 1000.0, 0.05, 2,
+                      seed=8)
+        else:
+            GENERATORS[name](R)
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:])

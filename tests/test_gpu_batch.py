@@ -115,3 +115,15 @@ def test_batch_of_identical_scenes_is_identical():
     first = _in_batch(bt, ids[0], a)
     for sid in ids[1:]:
         _assert_same("copy", _in_batch(bt, sid, a), first)
+
+
+def test_parameter_sweep_variants_match_alone():
+    from pcisph_gb300 import param_sweep
+    base = scenes.batch_dam(1500, 1.2, 0.8, d=0.01, seed=14)
+    vs = param_sweep.variants(base, viscosity=[0.1, 0.4], delta_t=[5e-4, 1e-3])
+    assert len(vs) == 4 and len({(v.viscosity, v.delta_t) for v in vs}) == 4
+    res = param_sweep.run(vs, steps=6, fields=FIELDS)
+    for v, r in zip(vs, res):
+        want = _alone(v, 6)
+        _assert_same(v.name, (r, (r["stats"].iterations, r["stats"].steps, r["stats"].total_iterations,
+                                  r["stats"].status_all)), want)

@@ -106,7 +106,7 @@ def _load_case(golden, case, **kw):
 
 
 @pytest.mark.parametrize("variant", [0, 1, 2])
-@pytest.mark.parametrize("case", ["step_boundary", "step_fluid"])
+@pytest.mark.parametrize("case", ["step_boundary", "step_fluid", "step_dambreak"])
 def test_kernel_chain_vs_reference(golden, case, variant):
     g, p, f = _load_case(golden, case, kernel_variant=variant)
     B = p.boundary_count
@@ -181,7 +181,7 @@ def test_boundary_self_density_computed(golden):
                      scale=p.density_variation_scaling_factor * p.rest_density)
 
 
-@pytest.mark.parametrize("case", ["step_boundary", "step_fluid"])
+@pytest.mark.parametrize("case", ["step_boundary", "step_fluid", "step_dambreak"])
 @pytest.mark.parametrize("loop_mode,variant", [(0, 2), (1, 2), (0, 0), (0, 1)])
 def test_full_steps_vs_reference(golden, case, loop_mode, variant):
     """Fluid::update sequence (min 3 / max 7 iterations, no walls) against the reference's full steps."""
@@ -443,3 +443,30 @@ def test_working_order_field_import_and_device_view():
     view = torch.as_tensor(View(ptr, n), device="cuda")
     np.testing.assert_array_equal(view.cpu().numpy(), want)
     f.close()
+
+
+@pytest.mark.parametrize("case", ["dam", "boundary"])
+def test_snapshot_restore_continues_exactly(tmp_path, golden, case):
+    """A checkpoint taken mid-run and restored into a new context continues bit for bit."""
+    from pcisph_gb300 import setup_scene
+    if case == "dam":
+        f = Fluid(0)
+        setup_scene(f, scenes.batch_drop(3000, d=0.01, seed=12), kernel_variant=2)
+    else:
+        g, p, f = _load_case(golden, "step_dambreak")
+    f.step(4)
+    path = tmp_path / "state.pcsnap"
+    f.save(path)
+    f.step(5)
+    want = {n: f.get_field(n) for n in ("position", "velocity", "density", "pressure")}
+    iters = f.stats().iterations
+    f.close()
+    h = Fluid(0)
+    h.load(path)
+    h.step(5)
+    for n, w in want.items():
+        np.testing.assert_array_equal(h.get_field(n), w, err_msg=n)
+    assert h.stats().iterations == iters
+    with pytest.raises(PcisphError):
+        h.restore(b"PCSN" + bytes(10))
+    h.close()

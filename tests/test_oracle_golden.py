@@ -67,7 +67,7 @@ def test_stable_sort_bit_exact(oracle, golden):
         i += 1
 
 
-@pytest.mark.parametrize("case", ["step_boundary", "step_fluid"])
+@pytest.mark.parametrize("case", ["step_boundary", "step_fluid", "step_dambreak"])
 def test_kernel_chain_bit_exact(oracle, golden, case):
     g = golden(case)
     p = params_from(g["params"])
@@ -113,7 +113,7 @@ def test_kernel_chain_bit_exact(oracle, golden, case):
     eq(x1, g["x_new"]); eq(v1, g["v_new"])
 
 
-@pytest.mark.parametrize("case", ["step_boundary", "step_fluid"])
+@pytest.mark.parametrize("case", ["step_boundary", "step_fluid", "step_dambreak"])
 def test_full_steps_bit_exact(oracle, golden, case):
     """Fluid::update sequence: reference settings (min 3, max 7 iterations, no walls, zero boundary self density)."""
     g = golden(case)

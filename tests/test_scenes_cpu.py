@@ -31,3 +31,14 @@ def test_drop_scene_has_pool_and_sphere():
 def test_batch_memory_model():
     per_particle, per_scene = memory_model()
     assert 400 < per_particle < 1000 and per_scene > 0
+
+
+def test_parameter_sweep_variants_are_a_product():
+    from pcisph_gb300 import param_sweep
+    base = scenes.small_dam(4)
+    vs = param_sweep.variants(base, viscosity=[0.1, 0.2, 0.3], surface_tension=[0.5, 1.0])
+    assert [(v.viscosity, v.surface_tension) for v in vs] == [(a, b) for a in (0.1, 0.2, 0.3) for b in (0.5, 1.0)]
+    assert base.viscosity == 0.2 and all(v.fluid_pos is base.fluid_pos for v in vs)
+    import pytest
+    with pytest.raises(ValueError):
+        param_sweep.variants(base, colour=[1])
