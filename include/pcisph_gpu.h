@@ -87,7 +87,8 @@ typedef struct pcisph_options {
                                       reference never launches that kernel (Fluid.cpp:167-171); 1: computed */
     int32_t loop_mode;             /* default 0: the corrective loop is decided on the device (CUDA graph with
                                       a conditional while node); 1: host reads the decision each iteration,
-                                      like the reference (Fluid.cpp:300-306) */
+                                      like the reference (Fluid.cpp:300-306); 2: the whole loop in one
+                                      persistent cooperative kernel (grid barriers between the sweeps) */
     int32_t kernel_variant;        /* neighbour sweeps. default 2: per-particle neighbour lists built by the
                                       density sweep (27-bucket walk), reused by the later sweeps of the step;
                                       0: one warp per bucket run with shared-memory staging; 1: one thread per
@@ -221,6 +222,21 @@ PCISPH_API int pcisph_run_stage(pcisph_ctx* ctx, int stage, int arg);
 /* Kernels launched by this context since creation (for launch accounting). */
 PCISPH_API uint64_t pcisph_kernel_launches(const pcisph_ctx* ctx);
 
+/* Autotuning. Times `steps` steps (after one warm-up step) of every candidate of variant 2's knobs --
+ * list skin 0.15, 0.2, 0.25, 0.3; working order on or off; radix digit width 6 or 8 bits -- from the
+ * current state, restores the state and the statistics after each, and keeps the fastest. Every candidate
+ * computes the same bits (the knobs change memory layout and list length, never a sum), so tuning leaves
+ * the simulation unchanged. Synchronises. No counterpart in the reference. */
+typedef struct pcisph_tune_result {
+    float list_skin;
+    int32_t spatial_order;
+    int32_t digit_bits;
+    float ms_per_step;          /* the chosen candidate */
+    float ms_per_step_before;   /* the settings on entry */
+    int32_t candidates;
+} pcisph_tune_result;
+PCISPH_API int pcisph_autotune(pcisph_ctx* ctx, uint32_t steps, pcisph_tune_result* out);
+
 /* Checkpoints. A snapshot is a self-describing host buffer: a header (magic "PCSN", format version, the
  * sizes of the parameter and option records, particle counts, threshold, steps taken), the parameter
  * setters' values, the options, then the fluid positions and velocities (float4 per particle, sorted
@@ -280,6 +296,9 @@ PCISPH_API int pcisph_batch_add_scene(pcisph_batch* batch, const pcisph_scene_de
 /* Removes a scene: its id is invalid at once; its particles leave the pool at the next step, which compacts
  * the pool once for all removals (stream-ordered device copies). */
 PCISPH_API int pcisph_batch_remove_scene(pcisph_batch* batch, int32_t scene_id);
+/* 0 (default): the corrective loop is a conditional WHILE node of the step's graph; 2: one persistent
+ * cooperative kernel runs it with per-scene convergence flags. Same results either way. */
+PCISPH_API int pcisph_batch_set_loop_mode(pcisph_batch* batch, int loop_mode);
 PCISPH_API int pcisph_batch_info(const pcisph_batch* batch, uint32_t* scenes, uint32_t* particles,
                                  uint32_t* free_particles);
 /* steps time steps of every scene (one CUDA graph launch each; no host synchronisation). */

@@ -73,6 +73,11 @@ class Camera(C.Structure):
                 ("fov_x_degrees", C.c_float)]
 
 
+class TuneResult(C.Structure):
+    _fields_ = [("list_skin", C.c_float), ("spatial_order", C.c_int32), ("digit_bits", C.c_int32),
+                ("ms_per_step", C.c_float), ("ms_per_step_before", C.c_float), ("candidates", C.c_int32)]
+
+
 class KernelTime(C.Structure):
     _fields_ = [("name", C.c_char * 32), ("launches", C.c_uint64), ("total_ms", C.c_double)]
 
@@ -140,6 +145,7 @@ def load():
         "pcisph_render": ([vp, vp, C.c_uint32, C.c_float, C.c_float, C.POINTER(Camera), i32, i32, vp, sz, vp, vp],
                           i32),
         "pcisph_render_fluid": ([vp, C.POINTER(Camera), i32, i32, vp, sz], i32),
+        "pcisph_autotune": ([vp, C.c_uint32, C.POINTER(TuneResult)], i32),
         "pcisph_snapshot_size": ([vp, C.POINTER(sz)], i32),
         "pcisph_snapshot": ([vp, vp, sz], i32),
         "pcisph_restore": ([vp, vp, sz], i32),
@@ -163,6 +169,7 @@ def load():
         "pcisph_batch_scene_stats": ([vp, C.c_int32, C.POINTER(StepStats)], i32),
         "pcisph_batch_get_field": ([vp, C.c_int32, i32, vp, sz, i32, i32], i32),
         "pcisph_batch_set_state": ([vp, C.c_int32, vp, vp, C.c_uint32, i32, i32], i32),
+        "pcisph_batch_set_loop_mode": ([vp, i32], i32),
         "pcisph_batch_kernel_launches": ([vp], C.c_uint64),
     }
     for name, (args, res) in sig.items():

@@ -40,12 +40,14 @@ def memory_model():
 
 
 class Batch:
-    def __init__(self, device=0, max_particles=1 << 20, max_scenes=256, stream=None):
+    def __init__(self, device=0, max_particles=1 << 20, max_scenes=256, stream=None, loop_mode=0):
         L = load()
         h = C.c_void_p()
         check(L.pcisph_batch_create(int(device), C.c_void_p(stream) if stream else None, int(max_particles),
                                     int(max_scenes), C.byref(h)))
         self._h, self._L = h, L
+        if loop_mode:
+            self.set_loop_mode(loop_mode)
 
     def close(self):
         if getattr(self, "_h", None):
@@ -80,6 +82,10 @@ class Batch:
         check(self._L.pcisph_batch_set_state(self._h, int(sid), C.c_void_p(pos.ctypes.data),
                                              None if vel is None else C.c_void_p(vel.ctypes.data),
                                              pos.shape[0], layout, _lib.MEM_HOST))
+
+    def set_loop_mode(self, mode):
+        """0: the corrective loop as a graph WHILE node; 2: one persistent cooperative kernel."""
+        check(self._L.pcisph_batch_set_loop_mode(self._h, int(mode)))
 
     def remove_scene(self, sid):
         check(self._L.pcisph_batch_remove_scene(self._h, int(sid)))

@@ -68,6 +68,7 @@ struct pcisph_batch {
     int32_t next_id = 1;
     uint32_t n_particles = 0, n_buckets = 0;
     int max_iters = 1;
+    int loop_mode = 0;   // 0: conditional WHILE node; 2: one persistent cooperative kernel
     bool dirty = false;  // scenes were added or removed since the tables were built
     cudaGraphExec_t graph_exec = nullptr;
     bool graph_valid = false;
@@ -142,7 +143,7 @@ struct pcisph_batch {
     ListBuffers list_buffers() const {
         return ListBuffers{pos, vel, pr4, normal, f_other, f_press, pred, pf4, state_pos, state_vel, rho, press, err,
                            cells, cells, nullptr, nullptr, nbr, nbr_count, near, near_count, bucket_fast,
-                           n_particles, nullptr};
+                           n_particles, nullptr, nullptr, nullptr};
     }
 
     uint32_t pool_end() const { return scenes.empty() ? 0u : scenes.back().offset + scenes.back().count; }
@@ -279,6 +280,29 @@ struct pcisph_batch {
                                                      cudaGetErrorString(e != cudaSuccess ? e : e2));
         }
         prefix_launches = nl;
+        if (loop_mode == 2) {  // the corrective loop as one cooperative kernel after the prefix
+            cudaGraph_t g2 = nullptr;
+            cudaGraphDestroy(graph);
+            BTRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+            const int nl2 = record_prefix(s);
+            const cudaError_t le = nl2 < 0 ? cudaSuccess
+                                           : launch_corrective_loop_scenes(scene_table(), list_buffers(), d_batch,
+                                                                           max_iters, s);
+            const cudaError_t ee = cudaStreamEndCapture(s, &g2);
+            if (nl2 < 0 || le != cudaSuccess || ee != cudaSuccess) {
+                if (g2) cudaGraphDestroy(g2);
+                return report_error(PCISPH_ERR_CUDA, std::string("graph capture of the persistent batch step failed: ") +
+                                                         cudaGetErrorString(le != cudaSuccess ? le : ee));
+            }
+            prefix_launches = nl2 + 1;
+            iter_launches = 0;
+            const cudaError_t ie = cudaGraphInstantiate(&graph_exec, g2, 0);
+            cudaGraphDestroy(g2);
+            if (ie != cudaSuccess) return report_error(PCISPH_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ie));
+            graph_valid = true;
+            return PCISPH_OK;
+        }
+        iter_launches = 3;
         cudaGraphConditionalHandle handle;
         BTRY(cudaGraphConditionalHandleCreate(&handle, graph, 1, cudaGraphCondAssignDefault));
         cudaGraphNodeParams cp{};
@@ -453,6 +477,16 @@ int pcisph_batch_remove_scene(pcisph_batch* b, int32_t id) {
     if (k < 0) return report_error(PCISPH_ERR_INVALID_ARG, "unknown scene id " + std::to_string(id));
     b->scenes[k].removed = true;  // compacted with every other removal at the next step
     b->dirty = true;
+    return PCISPH_OK;
+}
+
+int pcisph_batch_set_loop_mode(pcisph_batch* b, int loop_mode) {
+    if (!b) return report_error(PCISPH_ERR_INVALID_ARG, "batch is NULL");
+    if (loop_mode != 0 && loop_mode != 2) return report_error(PCISPH_ERR_INVALID_ARG, "batch loop_mode must be 0 or 2");
+    if (loop_mode != b->loop_mode) {
+        b->loop_mode = loop_mode;
+        b->graph_valid = false;
+    }
     return PCISPH_OK;
 }
 

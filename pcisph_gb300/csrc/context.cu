@@ -9,8 +9,10 @@
 //     by bucket_count;
 //   - the corrective loop is decided on the device; by default the whole step is
 //     one CUDA graph whose loop is a conditional WHILE node, so a step costs one
-//     graph launch and no host synchronisation (loop_mode 0). loop_mode 1 reads
-//     the decision back every iteration, as the reference does (Fluid.cpp:300-306).
+//     graph launch and no host synchronisation (loop_mode 0). loop_mode 2 puts the
+//     whole loop in one persistent cooperative kernel (list_kernels.cu) instead of
+//     the WHILE node. loop_mode 1 reads the decision back every iteration, as the
+//     reference does (Fluid.cpp:300-306).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -109,7 +111,7 @@ struct pcisph_ctx {
         return ListBuffers{b.pos, b.vel, b.pr4, b.normal, b.f_other, b.f_press, b.pred, b.pf4, b.state_pos,
                            b.state_vel, b.rho, b.press, b.err, w ? cells_w : b.cells, b.b_cells, b.b_pos, b.bpf,
                            b.nbr, b.nbr_count, b.near, b.near_count, b.bucket_fast, P.fluid_count,
-                           w ? d_of_w : nullptr};
+                           w ? d_of_w : nullptr, b.b_init, b.b_press};
     }
 
     // Working-order buffers for n particles and bk buckets; the index maps start as the identity.
@@ -436,7 +438,7 @@ struct pcisph_ctx {
     int record_iteration(cudaStream_t s, cudaGraphConditionalHandle cond, bool use_cond) {
         int nl = 0;
         if (params.boundary_count) {
-            timed("boundary_pressure", s, [&] { launch_boundary_pressure(P, b, s); });
+            timed("boundary_pressure", s, [&] { launch_boundary_pressure(P, b, working_order() ? cells_w : b.cells, s); });
             ++nl;
         }
         if (list_sweeps()) {
@@ -465,6 +467,23 @@ struct pcisph_ctx {
         cudaGraph_t graph = nullptr;
         CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
         int nl = record_prefix(s);
+        if (opts.loop_mode == 2) {  // persistent loop: prefix + one cooperative kernel, no conditional node
+            cudaError_t le = nl < 0 ? cudaSuccess : launch_corrective_loop(P, b.ctl, list_buffers(), s);
+            cudaError_t ee = cudaStreamEndCapture(s, &graph);
+            profiling = prof;
+            if (nl < 0 || le != cudaSuccess || ee != cudaSuccess) {
+                if (graph) cudaGraphDestroy(graph);
+                return fail(PCISPH_ERR_CUDA, std::string("graph capture of the persistent step failed: ") +
+                                                 cudaGetErrorString(le != cudaSuccess ? le : ee));
+            }
+            prefix_launches = nl + 1;
+            iter_launches = 0;
+            cudaError_t ie = cudaGraphInstantiate(&graph_exec, graph, 0);
+            cudaGraphDestroy(graph);
+            if (ie != cudaSuccess) return fail(PCISPH_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ie));
+            graph_valid = true;
+            return PCISPH_OK;
+        }
         cudaStreamCaptureStatus st;
         const cudaGraphNode_t* deps = nullptr;
         size_t ndeps = 0;
@@ -532,7 +551,7 @@ struct pcisph_ctx {
             rc = boundary_sort(s);
             if (rc) return rc;
         }
-        if (opts.loop_mode == 0 && !profiling) {
+        if (opts.loop_mode != 1 && !profiling) {
             if (!graph_valid) {
                 rc = build_graph();
                 if (rc) return rc;
@@ -547,6 +566,14 @@ struct pcisph_ctx {
         if (nl < 0) return fail(PCISPH_ERR_CUDA, std::string("step launch failed: ") + cudaGetErrorString(cudaGetLastError()));
         host_launches += nl;
         ++steps_launched;
+        if (opts.loop_mode == 2) {  // profiled persistent loop
+            cudaError_t le = cudaSuccess;
+            timed("corrective_loop", s, [&] { le = launch_corrective_loop(P, b.ctl, list_buffers(), s); });
+            if (le != cudaSuccess) return fail(PCISPH_ERR_CUDA, std::string("persistent loop: ") + cudaGetErrorString(le));
+            ++host_launches;
+            collect_timings();
+            return PCISPH_OK;
+        }
         const int lim = std::max(1, opts.max_iterations);
         for (int i = 0; i < lim; ++i) {
             host_launches += record_iteration(s, 0, false);
@@ -616,7 +643,7 @@ struct pcisph_ctx {
                 else launch_force(P, b, s);
                 ++host_launches;
                 break;
-            case PCISPH_STAGE_BOUNDARY_PRESSURE: launch_boundary_pressure(P, b, s); ++host_launches; break;
+            case PCISPH_STAGE_BOUNDARY_PRESSURE: launch_boundary_pressure(P, b, working_order() ? cells_w : b.cells, s); ++host_launches; break;
             case PCISPH_STAGE_PRESSURE:
                 if (list_sweeps()) launch_pressure_list(P, b.ctl, list_buffers(), s);
                 else if (warp_sweeps()) launch_pressure_sweep(P, b, sweep_args(), sweep_grid, s);
@@ -920,7 +947,9 @@ int pcisph_set_options(pcisph_ctx* ctx, const pcisph_options* o) {
     if (!ctx || !o) return fail(PCISPH_ERR_INVALID_ARG, "NULL argument");
     if (o->max_iterations < 1 || o->min_iterations < 1 || o->max_iterations > 10000)
         return fail(PCISPH_ERR_INVALID_ARG, "iteration limits must be in 1..10000");
-    if (o->loop_mode != 0 && o->loop_mode != 1) return fail(PCISPH_ERR_INVALID_ARG, "loop_mode must be 0 or 1");
+    if (o->loop_mode < 0 || o->loop_mode > 2) return fail(PCISPH_ERR_INVALID_ARG, "loop_mode must be 0, 1 or 2");
+    if (o->loop_mode == 2 && o->kernel_variant != 2)
+        return fail(PCISPH_ERR_INVALID_ARG, "loop_mode 2 (persistent loop) runs the list sweeps: kernel_variant 2");
     if (o->kernel_variant < 0 || o->kernel_variant > 2)
         return fail(PCISPH_ERR_INVALID_ARG, "kernel_variant must be 0, 1 or 2");
     if (!(o->list_skin >= 0.f && o->list_skin <= 2.f))
@@ -1174,6 +1203,111 @@ int pcisph_restore(pcisph_ctx* ctx, const void* src, size_t src_bytes) {
         rc = pcisph_set_boundary_state(ctx, f + (size_t)h.fluid_count * 8, h.boundary_count, PCISPH_LAYOUT_FLOAT4,
                                        PCISPH_MEM_HOST);
     return rc;
+}
+
+int pcisph_autotune(pcisph_ctx* ctx, uint32_t steps, pcisph_tune_result* out) {
+    if (!ctx || !out) return fail(PCISPH_ERR_INVALID_ARG, "NULL argument");
+    if (steps == 0 || steps > 1000) return fail(PCISPH_ERR_INVALID_ARG, "steps must be in 1..1000");
+    if (ctx->opts.kernel_variant != 2) return fail(PCISPH_ERR_INVALID_ARG, "autotuning covers kernel variant 2");
+    if (ctx->params_changed) {
+        int rc = ctx->derive_now();
+        if (rc) return rc;
+    }
+    int rc = ctx->check_consistent();
+    if (rc) return rc;
+    const uint32_t N = ctx->params.fluid_count;
+    if (N == 0) return fail(PCISPH_ERR_NOT_READY, "no particles to tune on");
+    DeviceGuard g(ctx->device);
+    cudaStream_t s = ctx->stream();
+    DeviceBlock saved;
+    if (saved.ensure((size_t)N * 32) != cudaSuccess) return fail(PCISPH_ERR_OOM, "device allocation for autotuning failed");
+    float4* sp = static_cast<float4*>(saved.p);
+    CUDA_TRY(cudaMemcpyAsync(sp, ctx->b.state_pos, (size_t)N * 16, cudaMemcpyDeviceToDevice, s));
+    CUDA_TRY(cudaMemcpyAsync(sp + N, ctx->b.state_vel, (size_t)N * 16, cudaMemcpyDeviceToDevice, s));
+    Control ctl0{};
+    CUDA_TRY(cudaStreamSynchronize(s));
+    CUDA_TRY(cudaMemcpy(&ctl0, ctx->ctl, sizeof(Control), cudaMemcpyDeviceToHost));
+    const uint64_t launches0 = ctx->host_launches, steps0 = ctx->steps_launched, iters0 = ctx->host_mode_iters;
+    const pcisph_options entry = ctx->opts;
+    const int entry_bits = ctx->sorter.digit_bits();
+    cudaEvent_t e0, e1;
+    CUDA_TRY(cudaEventCreate(&e0));
+    CUDA_TRY(cudaEventCreate(&e1));
+    auto restore = [&]() -> int {
+        CUDA_TRY(cudaMemcpyAsync(ctx->b.state_pos, sp, (size_t)N * 16, cudaMemcpyDeviceToDevice, s));
+        CUDA_TRY(cudaMemcpyAsync(ctx->b.state_vel, sp + N, (size_t)N * 16, cudaMemcpyDeviceToDevice, s));
+        CUDA_TRY(cudaMemcpyAsync(ctx->ctl, &ctl0, sizeof(Control), cudaMemcpyHostToDevice, s));
+        CUDA_TRY(cudaStreamSynchronize(s));
+        return PCISPH_OK;
+    };
+    auto apply = [&](float skin, int order, int bits) -> int {
+        pcisph_options o = ctx->opts;
+        o.list_skin = skin;
+        o.spatial_order = order;
+        int r = pcisph_set_options(ctx, &o);
+        if (r) return r;
+        ctx->sorter.set_digit_bits(bits);
+        ctx->sort_block.release();  // scratch size depends on the digit width
+        ctx->sorted_keys = ctx->f_keys;  // no view into the released scratch survives
+        ctx->sorted_ids = ctx->f_ids;
+        ctx->graph_valid = false;
+        return ctx->ensure_shared(std::max(N, ctx->boundary_cap_n));
+    };
+    auto time_it = [&](float* ms) -> int {
+        int r = restore();
+        if (!r) r = ctx->update();  // warm-up: builds the graph
+        if (!r) r = restore();
+        if (r) return r;
+        CUDA_TRY(cudaEventRecord(e0, s));
+        for (uint32_t k = 0; k < steps && !r; ++k) r = ctx->update();
+        CUDA_TRY(cudaEventRecord(e1, s));
+        CUDA_TRY(cudaEventSynchronize(e1));
+        if (r) return r;
+        CUDA_TRY(cudaEventElapsedTime(ms, e0, e1));
+        *ms /= (float)steps;
+        return PCISPH_OK;
+    };
+    float before = 0.f;
+    rc = apply(entry.list_skin, entry.spatial_order, entry_bits);
+    if (!rc) rc = time_it(&before);
+    float best_ms = before, best_skin = entry.list_skin;
+    int best_order = entry.spatial_order, best_bits = entry_bits, n = 1;
+    const float skins[] = {0.15f, 0.2f, 0.25f, 0.3f};
+    const int orders[] = {1, 0};
+    const int bits[] = {8, 6};
+    for (float sk : skins)
+        for (int od : orders)
+            for (int bt : bits) {
+                if (rc) break;
+                if (sk == entry.list_skin && od == entry.spatial_order && bt == entry_bits) continue;
+                float ms = 0.f;
+                rc = apply(sk, od, bt);
+                if (!rc) rc = time_it(&ms);
+                ++n;
+                if (!rc && ms < best_ms) {
+                    best_ms = ms;
+                    best_skin = sk;
+                    best_order = od;
+                    best_bits = bt;
+                }
+            }
+    if (!rc) rc = apply(best_skin, best_order, best_bits);
+    const int rc2 = restore();
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    saved.release();
+    ctx->host_launches = launches0;
+    ctx->steps_launched = steps0;
+    ctx->host_mode_iters = iters0;
+    if (rc) return rc;
+    if (rc2) return rc2;
+    out->list_skin = best_skin;
+    out->spatial_order = best_order;
+    out->digit_bits = best_bits;
+    out->ms_per_step = best_ms;
+    out->ms_per_step_before = before;
+    out->candidates = n;
+    return PCISPH_OK;
 }
 
 int pcisph_render_fluid(pcisph_ctx* ctx, const pcisph_camera* cam, int width, int height, uint8_t* rgb,

@@ -28,6 +28,10 @@
 // DevParams (own particle count, bucket count and base in the shared cell table, box, limits) and Control
 // live in device tables. Scenes stay contiguous in the sorted arrays because each scene's keys occupy its
 // own bucket range. k_batch_decide closes each iteration per scene; finished scenes skip the sweeps.
+#include <cooperative_groups.h>
+
+#include <algorithm>
+
 #include "list_kernels.cuh"
 #include "pair_terms.cuh"
 
@@ -247,9 +251,9 @@ __global__ void __launch_bounds__(kBlock) k_force_list(PS ps, ListBuffers b) {
 }
 
 // pcisph.cl:212-263 (boundary_update = 0); one scene: also the stop decision in the last block
+// One particle's pressure sweep; returns its density variation (0 when skipped or out of range).
 template <class PS>
-__global__ void __launch_bounds__(kBlock) k_pressure_list(PS ps, ListBuffers b) {
-    const uint32_t i = blockIdx.x * kBlock + threadIdx.x;
+__device__ __forceinline__ float pressure_body(const PS& ps, const ListBuffers& b, uint32_t i) {
     float dv = 0.f;
     if (i < ps.count() && !ps.skip_pressure(i)) {
         const DevParams& P = ps.params(i);
@@ -281,6 +285,12 @@ __global__ void __launch_bounds__(kBlock) k_pressure_list(PS ps, ListBuffers b) 
         b.pf4[i] = make_float4(xi.x, xi.y, xi.z, p / (r * r));
         if (PS::kBatched) warp_atomic_max(&ctl->max_err_bits, __float_as_uint(dv));
     }
+    return dv;
+}
+
+template <class PS>
+__global__ void __launch_bounds__(kBlock) k_pressure_list(PS ps, ListBuffers b) {
+    const float dv = pressure_body(ps, b, blockIdx.x * kBlock + threadIdx.x);
     if (PS::kBatched) return;
     // one scene: block max of dv, the last block decides (dv >= 0: bit patterns order like values)
     const unsigned bits = __reduce_max_sync(0xffffffffu, __float_as_uint(dv));
@@ -306,17 +316,10 @@ __global__ void __launch_bounds__(kBlock) k_pressure_list(PS ps, ListBuffers b) 
 }
 
 // pcisph.cl:265-300, then predict (pcisph.cl:175-193) or integrate with optional walls
+// One particle's pressure-force sweep, then predict (mode 0 before the decision, 1) or integrate (mode 0
+// after it, 2) with optional walls.
 template <class PS>
-__global__ void __launch_bounds__(kBlock) k_pressure_force_list(PS ps, ListBuffers b, int mode,
-                                                                cudaGraphConditionalHandle cond, int use_cond) {
-    const uint32_t i = blockIdx.x * kBlock + threadIdx.x;
-    if (!PS::kBatched && use_cond && i == 0) {
-        // continue the graph's while loop unless the step is done; the counter bounds it on its own
-        Control* ctl = ps.control(0);
-        const unsigned g = ++ctl->guard_iters;
-        const bool stop = ctl->done != 0u || g >= (unsigned)ps.params(0).max_iters;
-        cudaGraphSetConditional(cond, stop ? 0u : 1u);
-    }
+__device__ __forceinline__ void pressure_force_body(const PS& ps, const ListBuffers& b, uint32_t i, int mode) {
     if (i >= ps.count() || ps.skip_force(i)) return;
     const DevParams& P = ps.params(i);
     Control* ctl = ps.control(i);
@@ -362,6 +365,80 @@ __global__ void __launch_bounds__(kBlock) k_pressure_force_list(PS ps, ListBuffe
     const uint32_t o = b.out_index ? b.out_index[i] : i;  // working order -> sorted order
     b.state_pos[o] = f4(x, 0.f);
     b.state_vel[o] = f4(v, 0.f);
+}
+
+template <class PS>
+__global__ void __launch_bounds__(kBlock) k_pressure_force_list(PS ps, ListBuffers b, int mode,
+                                                                cudaGraphConditionalHandle cond, int use_cond) {
+    const uint32_t i = blockIdx.x * kBlock + threadIdx.x;
+    if (!PS::kBatched && use_cond && i == 0) {
+        // continue the graph's while loop unless the step is done; the counter bounds it on its own
+        Control* ctl = ps.control(0);
+        const unsigned g = ++ctl->guard_iters;
+        const bool stop = ctl->done != 0u || g >= (unsigned)ps.params(0).max_iters;
+        cudaGraphSetConditional(cond, stop ? 0u : 1u);
+    }
+    pressure_force_body(ps, b, i, mode);
+}
+
+// The corrective loop of one step as one cooperative launch (every block resident, grid-stride over the
+// particles): pressure sweep, grid barrier, the loop decision in block 0 (one scene, or every scene of a
+// batch with its own convergence flags), grid barrier, pressure-force sweep, grid barrier; until no scene
+// iterates, at most max_iters times. Same sweeps and decisions as the graph's while loop, so the same bits.
+// Every thread takes every barrier: the bodies return to the loop, never out of the kernel.
+template <class PS>
+__global__ void __launch_bounds__(kBlock) k_corrective_loop(PS ps, ListBuffers b, Control* loop, int max_iters) {
+    namespace cg = cooperative_groups;
+    cg::grid_group grid = cg::this_grid();
+    const uint32_t stride = gridDim.x * kBlock;
+    const uint32_t rounds = (ps.count() + stride - 1) / stride;
+    __shared__ int running;
+    for (int it = 0; it < max_iters; ++it) {
+        if constexpr (!PS::kBatched) {  // boundary pressures at the predicted positions (read by the force)
+            const DevParams& P = ps.params(0);
+            for (uint32_t k = blockIdx.x * kBlock + threadIdx.x; k < P.boundary_count; k += stride)
+                boundary_pressure_body(P, b.cells, b.pred, b.b_pos, b.b_init, b.b_press, const_cast<float4*>(b.bpf), k);
+        }
+        unsigned local = 0;
+        for (uint32_t r = 0; r < rounds; ++r)
+            local = max(local, __float_as_uint(pressure_body(ps, b, r * stride + blockIdx.x * kBlock + threadIdx.x)));
+        if (!PS::kBatched) {  // batched scenes reduced per scene inside the body
+            const unsigned m = __reduce_max_sync(0xffffffffu, local);
+            if ((threadIdx.x & 31) == 0 && m) atomicMax(&ps.control(0)->max_err_bits, m);
+        }
+        grid.sync();
+        if (blockIdx.x == 0) {
+            if (threadIdx.x == 0) running = 0;
+            __syncthreads();
+            if constexpr (!PS::kBatched) {
+                if (threadIdx.x == 0) {
+                    Control* c = ps.control(0);
+                    decide(ps.params(0), c);
+                    running = c->done ? 0 : 1;
+                }
+            } else {
+                for (uint32_t sc = threadIdx.x; sc < ps.n_scenes; sc += blockDim.x) {
+                    Control* c = &ps.ctls[sc];
+                    if (c->done) {
+                        c->finished = 1;
+                        continue;
+                    }
+                    decide(ps.table[sc], c);
+                    if (!c->done) atomicOr(&running, 1);
+                }
+            }
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                loop->guard_iters += 1;
+                if (PS::kBatched) loop->total_iters += 1;
+                loop->any_running = running ? 1u : 0u;
+            }
+        }
+        grid.sync();
+        for (uint32_t r = 0; r < rounds; ++r) pressure_force_body(ps, b, r * stride + blockIdx.x * kBlock + threadIdx.x, 0);
+        grid.sync();
+        if (*reinterpret_cast<volatile unsigned*>(&loop->any_running) == 0u) break;
+    }
 }
 
 // Batch: close one corrective iteration per scene (one thread per scene) and set the graph's loop
@@ -452,6 +529,39 @@ void launch_pressure_force_list(const DevParams& P, Control* ctl, const ListBuff
                                 cudaGraphConditionalHandle cond, bool use_cond, cudaStream_t s) {
     k_pressure_force_list<<<grid_for(P.fluid_count), kBlock, 0, s>>>(OneScene{P, ctl}, b, mode, cond,
                                                                       use_cond ? 1 : 0);
+}
+
+namespace {
+template <class PS>
+cudaError_t launch_loop(const PS& ps, uint32_t n, const ListBuffers& b, Control* loop, int max_iters, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    int dev = 0, sms = 0, per_sm = 0, coop = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_corrective_loop<PS>, kBlock, 0);
+    if (e != cudaSuccess) return e;
+    if (!coop || per_sm < 1) return cudaErrorNotSupported;
+    const unsigned blocks = std::min<unsigned>((unsigned)(sms * per_sm), grid_for(n));
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(blocks);
+    cfg.blockDim = dim3(kBlock);
+    cfg.stream = s;
+    cudaLaunchAttribute attr{};
+    attr.id = cudaLaunchAttributeCooperative;
+    attr.val.cooperative = 1;
+    cfg.attrs = &attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k_corrective_loop<PS>, ps, b, loop, max_iters);
+}
+}  // namespace
+
+cudaError_t launch_corrective_loop(const DevParams& P, Control* ctl, const ListBuffers& b, cudaStream_t s) {
+    return launch_loop(OneScene{P, ctl}, P.fluid_count, b, ctl, P.max_iters, s);
+}
+cudaError_t launch_corrective_loop_scenes(const SceneTable& t, const ListBuffers& b, Control* batch, int max_iters,
+                                          cudaStream_t s) {
+    return launch_loop(t, t.n, b, batch, max_iters, s);
 }
 
 void launch_batch_begin(Control* ctls, uint32_t n_scenes, Control* batch, cudaStream_t s) {

@@ -23,6 +23,8 @@ struct ListBuffers {
     unsigned char* bucket_fast;  // per bucket of the cell table: holds a fast particle this step
     uint32_t nbr_stride;         // particles in the arrays (>= every index i)
     const uint32_t* out_index;   // integration writes particle i's state at out_index[i] (null: at i)
+    const float* b_init;         // boundary initial (self) densities and pressures (single scene, B > 0)
+    float* b_press;
 };
 
 // One scene: parameters by value; the pressure kernel's last block decides the loop.
@@ -70,6 +72,11 @@ void launch_normal_scenes(const SceneTable& t, const ListBuffers& b, cudaStream_
 void launch_force_scenes(const SceneTable& t, const ListBuffers& b, cudaStream_t s);
 void launch_pressure_scenes(const SceneTable& t, const ListBuffers& b, cudaStream_t s);
 void launch_pressure_force_scenes(const SceneTable& t, const ListBuffers& b, cudaStream_t s);
+// The whole corrective loop of a step in one cooperative launch (loop_mode 2); errors if the device cannot
+// run it (cooperative launch unsupported).
+cudaError_t launch_corrective_loop(const DevParams& P, Control* ctl, const ListBuffers& b, cudaStream_t s);
+cudaError_t launch_corrective_loop_scenes(const SceneTable& t, const ListBuffers& b, Control* batch, int max_iters,
+                                          cudaStream_t s);
 // per-scene loop decision; sets the while-loop condition (continue while a scene iterates)
 void launch_batch_decide(const SceneTable& t, Control* batch, int max_iters, cudaGraphConditionalHandle cond,
                          bool use_cond, cudaStream_t s);

@@ -75,4 +75,33 @@ __device__ __forceinline__ void pressure_force_term(const float4& xi, const floa
     }
 }
 
+// One boundary particle's pressure update at the predicted fluid positions (pcisph.cl:212-263 with
+// boundary_update = 1): predicted density from its initial (self) density plus the fluid neighbours,
+// pressure increment delta * max(0, rho* - rho0), and its packed operand (x_b, p_b / rho0^2) for the
+// pressure force. cells: the fluid cell table in the order pred is stored in.
+__device__ __forceinline__ void boundary_pressure_body(const DevParams& P, const uint2* __restrict__ cells,
+                                                       const float4* __restrict__ pred,
+                                                       const float4* __restrict__ b_pos,
+                                                       const float* __restrict__ b_init, float* __restrict__ b_press,
+                                                       float4* __restrict__ bpf, uint32_t i) {
+    if (i >= P.boundary_count) return;
+    const float4 xb = b_pos[i];
+    const Cell c = cell_of(xb.x, xb.y, xb.z, P);
+    float acc = b_init[i];
+    for_each_neighbour(cells, c, P, [&](uint32_t j) {
+        const float4 o = __ldg(&pred[j]);
+        const float dx = xb.x - o.x, dy = xb.y - o.y, dz = xb.z - o.z;
+        acc += poly6(dist2(dx, dy, dz), P.h2);
+    });
+    acc *= P.particle_mass * P.poly6_norm;
+    float dv = acc - P.rest_density;
+    dv = 0.f < dv ? dv : 0.f;
+    float p = b_press[i];
+    if (dv != 0.f) {
+        p += dv * P.delta;
+        b_press[i] = p;
+    }
+    bpf[i] = make_float4(xb.x, xb.y, xb.z, p / (P.rest_density * P.rest_density));
+}
+
 }  // namespace pcisph

@@ -188,25 +188,7 @@ __global__ void __launch_bounds__(kBlock) k_boundary_pressure(DevParams P, const
                                                               const float* __restrict__ b_init,
                                                               float* __restrict__ b_press,
                                                               float4* __restrict__ bpf) {
-    const uint32_t i = blockIdx.x * kBlock + threadIdx.x;
-    if (i >= P.boundary_count) return;
-    const float4 xb = b_pos[i];
-    const Cell c = cell_of(xb.x, xb.y, xb.z, P);
-    float acc = b_init[i];
-    for_each_neighbour(cells, c, P, [&](uint32_t j) {
-        const float4 o = __ldg(&pred[j]);
-        const float dx = xb.x - o.x, dy = xb.y - o.y, dz = xb.z - o.z;
-        acc += poly6(dist2(dx, dy, dz), P.h2);
-    });
-    acc *= P.particle_mass * P.poly6_norm;
-    float dv = acc - P.rest_density;
-    dv = 0.f < dv ? dv : 0.f;
-    float p = b_press[i];
-    if (dv != 0.f) {
-        p += dv * P.delta;
-        b_press[i] = p;
-    }
-    bpf[i] = make_float4(xb.x, xb.y, xb.z, p / (P.rest_density * P.rest_density));
+    boundary_pressure_body(P, cells, pred, b_pos, b_init, b_press, bpf, blockIdx.x * kBlock + threadIdx.x);
 }
 
 // pcisph.cl:212-263 with boundary_update = 0, plus the stop decision (Fluid.cpp:284-306)
@@ -419,9 +401,9 @@ void launch_boundary_self_density(const DevParams& P, const StepBuffers& b, cuda
     k_boundary_self_density<<<grid_for(P.boundary_count), kBlock, 0, s>>>(P, b.b_cells, b.b_pos, b.b_init);
 }
 
-void launch_boundary_pressure(const DevParams& P, const StepBuffers& b, cudaStream_t s) {
+void launch_boundary_pressure(const DevParams& P, const StepBuffers& b, const uint2* cells, cudaStream_t s) {
     if (!P.boundary_count) return;
-    k_boundary_pressure<<<grid_for(P.boundary_count), kBlock, 0, s>>>(P, b.cells, b.pred, b.b_pos, b.b_init,
+    k_boundary_pressure<<<grid_for(P.boundary_count), kBlock, 0, s>>>(P, cells, b.pred, b.b_pos, b.b_init,
                                                                        b.b_press, b.bpf);
 }
 

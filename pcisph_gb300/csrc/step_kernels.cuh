@@ -49,7 +49,8 @@ void launch_density(const DevParams& P, const StepBuffers& b, cudaStream_t s);
 void launch_normal(const DevParams& P, const StepBuffers& b, cudaStream_t s);
 void launch_force(const DevParams& P, const StepBuffers& b, cudaStream_t s);
 void launch_boundary_self_density(const DevParams& P, const StepBuffers& b, cudaStream_t s);
-void launch_boundary_pressure(const DevParams& P, const StepBuffers& b, cudaStream_t s);
+// cells: the fluid cell table in the order b.pred is stored in (sorted or working order)
+void launch_boundary_pressure(const DevParams& P, const StepBuffers& b, const uint2* cells, cudaStream_t s);
 void launch_pressure(const DevParams& P, const StepBuffers& b, cudaStream_t s);
 // mode 0: the loop decision in ctl picks predict or integrate; 1: predict; 2: integrate.
 // With use_cond, thread 0 also sets the graph's while-loop condition (continue unless done or max_iters).

@@ -127,3 +127,19 @@ def test_parameter_sweep_variants_match_alone():
         want = _alone(v, 6)
         _assert_same(v.name, (r, (r["stats"].iterations, r["stats"].steps, r["stats"].total_iterations,
                                   r["stats"].status_all)), want)
+
+
+def test_persistent_loop_batch_matches_graph_loop():
+    """loop_mode 2 runs the corrective loop as one cooperative kernel with per-scene flags: same bits as
+    the graph's WHILE node, scene by scene."""
+    sc = _mixed_scenes()
+    out = []
+    for mode in (0, 2):
+        bt = Batch(0, max_particles=sum(s.fluid_count for s in sc), max_scenes=len(sc), loop_mode=mode)
+        ids = [bt.add_scene(s) for s in sc]
+        bt.step(8)
+        bt.sync()
+        out.append([_in_batch(bt, i, s) for i, s in zip(ids, sc)])
+        bt.close()
+    for s, a, b in zip(sc, out[0], out[1]):
+        _assert_same(s.name, b, a)

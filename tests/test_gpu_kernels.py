@@ -166,8 +166,13 @@ def test_kernel_chain_vs_reference(golden, case, variant):
     print(case, variant, {k: f"{v:.1e}" for k, v in errs.items()})
 
 
-def test_boundary_self_density_computed(golden):
-    g, p, f = _load_case(golden, "step_boundary", boundary_self_density=1)
+@pytest.mark.parametrize("variant", [1, 2])
+@pytest.mark.parametrize("case", ["step_boundary", "step_dambreak"])
+def test_boundary_self_density_computed(golden, case, variant):
+    """Boundary pressures with the boundary self density computed (the reference's never-launched kernel,
+    pcisph.cl:195-210): in the reference dambreak they are non-zero, so the predicted positions must be
+    read through the cell table of the order they are stored in."""
+    g, p, f = _load_case(golden, case, boundary_self_density=1, kernel_variant=variant)
     f.run_stage("sort")
     assert_close("boundary_init_density", f.get_field("boundary_init_density"), g["b_init"])
     f.run_stage("density")
@@ -182,7 +187,7 @@ def test_boundary_self_density_computed(golden):
 
 
 @pytest.mark.parametrize("case", ["step_boundary", "step_fluid", "step_dambreak"])
-@pytest.mark.parametrize("loop_mode,variant", [(0, 2), (1, 2), (0, 0), (0, 1)])
+@pytest.mark.parametrize("loop_mode,variant", [(0, 2), (1, 2), (2, 2), (0, 0), (0, 1)])
 def test_full_steps_vs_reference(golden, case, loop_mode, variant):
     """Fluid::update sequence (min 3 / max 7 iterations, no walls) against the reference's full steps."""
     g, p, f = _load_case(golden, case, loop_mode=loop_mode, kernel_variant=variant)
@@ -207,16 +212,17 @@ def test_full_steps_vs_reference(golden, case, loop_mode, variant):
 def test_graph_and_host_loop_identical(variant):
     sc = scenes.small_dam(10, seed=3)
     out = []
-    for mode in (0, 1):
+    for mode in ((0, 1, 2) if variant == 2 else (0, 1)):
         f = Fluid(0)
         from pcisph_gb300 import setup_scene
         setup_scene(f, sc, loop_mode=mode, kernel_variant=variant)
         f.step(5)
         st = f.stats()
         out.append((f.get_field("position"), f.get_field("velocity"), f.get_field("pressure"), st.total_iterations))
-    for a, b in zip(out[0][:3], out[1][:3]):
-        np.testing.assert_array_equal(a, b)
-    assert out[0][3] == out[1][3]
+    for other in out[1:]:
+        for a, b in zip(out[0][:3], other[:3]):
+            np.testing.assert_array_equal(a, b)
+        assert out[0][3] == other[3]
 
 
 # ------------------------------------------------------------------------------------------- full step vs FP64
@@ -470,3 +476,27 @@ def test_snapshot_restore_continues_exactly(tmp_path, golden, case):
     with pytest.raises(PcisphError):
         h.restore(b"PCSN" + bytes(10))
     h.close()
+
+
+def test_autotune_leaves_the_simulation_unchanged():
+    """Autotuning restores the state after every candidate and picks among settings that compute the same
+    bits, so a tuned run continues exactly like an untuned one."""
+    from pcisph_gb300 import setup_scene
+    sc = scenes.batch_drop(6000, d=0.01, seed=15)
+    out = []
+    for tune in (False, True):
+        f = Fluid(0)
+        setup_scene(f, sc, kernel_variant=2)
+        f.step(3)
+        if tune:
+            r = f.autotune(steps=2)
+            assert r["candidates"] == 16 and r["ms_per_step"] <= r["ms_per_step_before"]
+            assert f.get_options().list_skin == pytest.approx(r["list_skin"])
+        f.step(5)
+        st = f.stats()
+        out.append(({n: f.get_field(n) for n in ("position", "velocity", "density")},
+                    (st.steps, st.total_iterations, st.status_all)))
+        f.close()
+    for n in out[0][0]:
+        np.testing.assert_array_equal(out[1][0][n], out[0][0][n], err_msg=n)
+    assert out[0][1] == out[1][1]
