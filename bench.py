@@ -42,6 +42,17 @@ ALGO_BYTES = {
     "hash": 20,             # x 12 + key 4 + id 4
     "radix_sort": 48,       # 3 passes of 8 B read + 8 B written
 }
+DAM_WORKLOADS = {
+    "dam1m": ("config1", "particle-steps/s @1M (<=1% rho err)",
+              "dam break 128x128x64 = 1,048,576 particles, d=0.005 m, dt=2.5e-4 s, reflecting walls, "
+              "3-50 corrective iterations to <1% density error"),
+    "dam32k": ("config0", "particle-steps/s @32K (<=1% rho err)",
+               "dam break 32^3 = 32,768 particles, d=0.02 m, dt=1e-3 s, reflecting walls, "
+               "3-50 corrective iterations to <1% density error"),
+    "dam8m": ("config2", "particle-steps/s @8M (<=1% rho err)",
+              "two 256x128x128 blocks = 8,388,608 particles, d=0.0025 m, dt=1.25e-4 s, reflecting walls, "
+              "3-50 corrective iterations to <1% density error"),
+}
 WORKLOAD = ("dam break 128x128x64 = 1,048,576 particles, d=0.005 m, dt=2.5e-4 s, reflecting walls, "
             "3-50 corrective iterations to <1% density error")
 
@@ -54,14 +65,17 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=20.0, help="bound of the CPU baseline sample")
     ap.add_argument("--variant", type=int, default=2, help="neighbour-sweep kernel variant (pcisph_options)")
-    ap.add_argument("--workload", default="dam1m", choices=["dam1m", "scenes", "serve"],
-                    help="dam1m: the 1M-particle dam break (the headline); scenes: 256 scenes batched vs "
+    ap.add_argument("--workload", default="dam1m", choices=["dam1m", "dam32k", "dam8m", "scenes", "serve"],
+                    help="dam1m: the 1M-particle dam break (the headline); dam32k / dam8m: the 32K and 8M "
+                         "dam breaks; scenes: 256 scenes batched vs "
                          "stepped one context each; serve: Poisson requests through the serving loop")
     ap.add_argument("--requests", type=int, default=20000, help="request count of --workload serve")
     ap.add_argument("--rate", type=float, default=200.0, help="arrivals per second of --workload serve")
     ap.add_argument("--budget-gb", type=float, default=100.0, help="device memory budget of --workload serve")
     ap.add_argument("--duration", type=float, default=120.0, help="wall-time bound (s) of --workload serve")
     ap.add_argument("--scenes", type=int, default=256, help="scene count of --workload scenes")
+    ap.add_argument("--loop-mode", type=int, default=0, choices=[0, 2],
+                    help="corrective loop: 0 graph WHILE node, 2 persistent cooperative kernel")
     return ap.parse_args()
 
 
@@ -166,7 +180,8 @@ def reference_arm(args, rank, world):
         return
     from pcisph_gb300 import scenes
     import numpy as np
-    sc = scenes.config1()
+    cfg, metric, workload = DAM_WORKLOADS.get(args.workload, DAM_WORKLOADS["dam1m"])
+    sc = getattr(scenes, cfg)()
     pos, vel = sc.fluid_pos, np.zeros_like(sc.fluid_pos)
     w = min(args.warmup, 3)
     if w:
@@ -175,11 +190,11 @@ def reference_arm(args, rank, world):
     rate, steps, iters, _ = cpu_step_rate(sc, pos, vel, args.cpu_seconds * 2, max_steps=args.steps)
     cores = os.cpu_count()
     line = {
-        "impl": "reference", "metric": "particle-steps/s @1M (<=1% rho err)", "value": rate,
+        "impl": "reference", "metric": metric, "value": rate,
         "unit": "particle-steps/s", "n_gpus": 0, "steps": steps, "warmup": w, "ms_per_step": 1e3 * sc.fluid_count / rate,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded jittered lattice)",
-        "config": {"workload": WORKLOAD, "particles": sc.fluid_count, "mean_iterations": iters},
+        "config": {"workload": workload, "particles": sc.fluid_count, "mean_iterations": iters},
         "cpu_baseline": {"value": rate, "unit": "particle-steps/s", "cores": cores, "kind": "port",
                          "sample": f"{sc.fluid_count} particles x {steps} steps after {w} warm-up steps "
                                    f"(oracle/pcisph_oracle.cpp, OpenMP over particles; the reference's OpenCL "
@@ -230,7 +245,7 @@ def scenes_workload(args, rank, world, local):
         return ms
 
     # batched: every scene in one pool, one graph launch per step
-    bt = Batch(local, max_particles=n_total, max_scenes=len(sc), stream=stream.cuda_stream)
+    bt = Batch(local, max_particles=n_total, max_scenes=len(sc), stream=stream.cuda_stream, loop_mode=args.loop_mode)
     ids = [bt.add_scene(s) for s in sc]
     for _ in range(args.warmup):
         bt.step(1)
@@ -305,6 +320,7 @@ def scenes_workload(args, rank, world, local):
                        "parallelism": f"scenes sharded over {world} GPU(s)",
                        "scene_steps_per_s": len(all_sc) * args.steps / (ms_batch / 1e3),
                        "mean_scene_iterations": float(np.mean(iters)), "batch_loop_iterations": batch_loop_iters,
+                       "loop_mode": args.loop_mode,
                        "l2": "working set ~6 GB > L2"},
             "per_scene_contexts": {"value": n_all * args.steps / (ms_single / 1e3), "unit": "particle-steps/s",
                                    "ms_per_step": ms_single / args.steps, "gpu_launches": single_launches,
@@ -339,7 +355,8 @@ def serve_workload(args, rank, world, local):
     max_scenes = min(65535, max(16, budget // (2048 * bpp + bps)))
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
-    bt = Batch(local, max_particles=max_particles, max_scenes=max_scenes, stream=stream.cuda_stream)
+    bt = Batch(local, max_particles=max_particles, max_scenes=max_scenes, stream=stream.cuda_stream,
+               loop_mode=args.loop_mode)
     srv = Server(bt, budget, bpp, bps, max_particles, max_scenes, keep_state=True)
     # warm-up: one small request served to completion before the clock starts (graph build, first launches)
     Server(bt, budget, bpp, bps, max_particles, max_scenes, keep_state=False).run(reqs[:1], realtime=False)
@@ -350,6 +367,7 @@ def serve_workload(args, rank, world, local):
     rep = srv.run(reqs, duration=args.duration, realtime=True)
     clocks = sampler.stop()
     summ = rep.summary()
+    summ["graph_instantiations"], summ["graph_updates"] = bt.graph_stats()
     if world > 1:
         got = [None] * world
         dist.all_gather_object(got, summ)
@@ -358,8 +376,8 @@ def serve_workload(args, rank, world, local):
     if rank == 0:
         wall = max(g["wall_s"] for g in got)
         ps = sum(g["particle_steps_per_s"] * g["wall_s"] for g in got)
-        offered = sum(r.particles * r.steps for r in poisson_requests(min(horizon, 2000), args.rate, seed=4)) / \
-            min(horizon, 2000) * args.rate
+        sample = poisson_requests(min(horizon, 5000), args.rate, seed=4)
+        offered = sum(r.spec[1] * r.steps for r in sample) / len(sample) * args.rate  # target counts
         line = {
             "metric": "particle-steps/s served", "value": ps / wall, "unit": "particle-steps/s", "n_gpus": world,
             "steps": summ["batch_steps"], "warmup": 1, "ms_per_step": summ["step_ms_p50"],
@@ -403,12 +421,13 @@ def main():
     torch.cuda.set_device(local)
     from pcisph_gb300 import Fluid, build, scenes, setup_scene
     build.build()
-    sc = scenes.config1()
+    cfg, metric, workload = DAM_WORKLOADS[args.workload]
+    sc = getattr(scenes, cfg)()
     N = sc.fluid_count
     stream = torch.cuda.Stream()  # a real stream: the library launches on it, the events are recorded on it
     torch.cuda.set_stream(stream)
     f = Fluid(local, stream=stream.cuda_stream)
-    setup_scene(f, sc, kernel_variant=args.variant)
+    setup_scene(f, sc, kernel_variant=args.variant, loop_mode=args.loop_mode)
     sampler = ClockSampler(local)
     sampler.start()
     for _ in range(args.warmup):
@@ -455,20 +474,25 @@ def main():
     # per-kernel CUDA events over the first steps of the timed loop again (host-driven loop, same kernels)
     prof_steps = min(args.steps, 20)
     f.set_fluid_state(snap_pos, snap_vel)
+    sp0 = f.stats()
     f.profile(True)
     f.step(prof_steps)
     prof = f.profile_read()
     f.profile(False)
+    sp1 = f.stats()
+    prof_iters = (sp1.total_iterations - sp0.total_iterations) / max(1, sp1.steps - sp0.steps)
     clocks = sampler.stop()
     tot = sum(ms for _, ms in prof.values())
     dom = max(prof.items(), key=lambda kv: kv[1][1])
     dname, (dl, dms) = dom
     avg_s = dms / dl / 1e3
     peak, peak_kind = peaks()
-    achieved = ALGO_BYTES.get(dname, 0) * N / avg_s / 1e9
+    # the persistent loop (loop_mode 2) runs a step's iterations in one launch
+    algo = dict(ALGO_BYTES, corrective_loop=(ALGO_BYTES["pressure"] + ALGO_BYTES["pressure_force"]) * prof_iters)
+    achieved = algo.get(dname, 0) * N / avg_s / 1e9
     traffic = ncu_traffic(args.variant).get(dname)
     kernels = {k: {"launches": l, "avg_us": 1e3 * ms / l, "share": ms / tot,
-                   "algo_GBps": ALGO_BYTES.get(k, 0) * N / (ms / l / 1e3) / 1e9} for k, (l, ms) in prof.items()}
+                   "algo_GBps": algo.get(k, 0) * N / (ms / l / 1e3) / 1e9} for k, (l, ms) in prof.items()}
 
     # e2e through the C ABI with pinned host buffers, over the same first steps
     pos_h = torch.empty((N, 3), dtype=torch.float32, pin_memory=True).numpy()
@@ -492,18 +516,18 @@ def main():
 
     cpu = None
     if rank == 0 and world == 1:
-        rate, csteps, citers, _ = cpu_step_rate(sc, start_pos, start_vel, args.cpu_seconds)
+        rate, csteps, citers, _ = cpu_step_rate(sc, start_pos, start_vel, args.cpu_seconds, max_steps=args.steps)
         cpu = {"value": rate, "unit": "particle-steps/s", "cores": os.cpu_count(), "kind": "port",
                "sample": f"{N} particles x the first {csteps} of the timed steps, from the same state "
                          f"(mean {citers:.2f} corrective iterations), oracle/pcisph_oracle.cpp with OpenMP"}
     if rank == 0:
         line = {
-            "metric": "particle-steps/s @1M (<=1% rho err)", "value": value, "unit": "particle-steps/s",
+            "metric": metric, "value": value, "unit": "particle-steps/s",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded jittered lattice)",
-            "config": {"workload": WORKLOAD, "particles": N, "parallelism": f"replicas x{world}",
-                       "kernel_variant": args.variant,
+            "config": {"workload": workload, "particles": N, "parallelism": f"replicas x{world}",
+                       "kernel_variant": args.variant, "loop_mode": args.loop_mode,
                        "mean_iterations": iters, "max_density_error_last": st1.max_density_error,
                        "step_ms_min_median_max": [min(step_ms), statistics.median(step_ms), max(step_ms)],
                        "converged_all_steps": (status_bits & 1) == 0, "status_bits": status_bits,
@@ -514,7 +538,8 @@ def main():
             "roofline": {"bound": "hbm", "kernel": dname, "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_kind": peak_kind,
                          "traffic": traffic * N if traffic else None,
-                         "algo_bytes_per_particle": ALGO_BYTES.get(dname, 0), "avg_launch_us": avg_s * 1e6},
+                         "algo_bytes_per_particle": algo.get(dname, 0), "avg_launch_us": avg_s * 1e6,
+                         "profile_pass_iterations_per_step": prof_iters},
             "kernels": kernels,
             "cpu_baseline": cpu,
             "clocks": clocks,

@@ -94,9 +94,10 @@ typedef struct pcisph_options {
                                       0: one warp per bucket run with shared-memory staging; 1: one thread per
                                       particle walking the 27 buckets in every sweep */
     float list_skin;               /* variant 2: list radius = kernel_radius * (1 + list_skin), default 0.25 */
-    int32_t spatial_order;         /* variant 2, default 1: the sweeps run in a working order that places
-                                      whole buckets in Morton order of their cells (every sum unchanged; state
-                                      and exported fields stay in the reference's sorted order); 0: sorted order */
+    int32_t spatial_order;         /* variant 2: 1, the sweeps run in a working order that places whole
+                                      buckets in Morton order of their cells (every sum unchanged; state and
+                                      exported fields stay in the reference's sorted order); 0: sorted order;
+                                      2 (default): 1 from 131,072 particles, else 0 */
 } pcisph_options;
 
 typedef struct pcisph_step_stats {
@@ -314,6 +315,8 @@ PCISPH_API int pcisph_batch_set_state(pcisph_batch* batch, int32_t scene_id, con
 PCISPH_API int pcisph_batch_get_field(pcisph_batch* batch, int32_t scene_id, int field, void* dst,
                                       size_t dst_bytes, int layout, int memory);
 PCISPH_API uint64_t pcisph_batch_kernel_launches(const pcisph_batch* batch);
+/* Step graphs instantiated, and updated in place after a change of composition, since creation. */
+PCISPH_API int pcisph_batch_graph_stats(const pcisph_batch* batch, uint64_t* instantiations, uint64_t* updates);
 
 /* ------------------------------------------------------------ rendering */
 /* Headless replacement of the reference's OpenGL particle rendering (vis/fluid_rendering.cpp:65-103 with

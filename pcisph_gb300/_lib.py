@@ -170,6 +170,7 @@ def load():
         "pcisph_batch_get_field": ([vp, C.c_int32, i32, vp, sz, i32, i32], i32),
         "pcisph_batch_set_state": ([vp, C.c_int32, vp, vp, C.c_uint32, i32, i32], i32),
         "pcisph_batch_set_loop_mode": ([vp, i32], i32),
+        "pcisph_batch_graph_stats": ([vp, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)], i32),
         "pcisph_batch_kernel_launches": ([vp], C.c_uint64),
     }
     for name, (args, res) in sig.items():

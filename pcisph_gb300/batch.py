@@ -106,6 +106,12 @@ class Batch:
         check(self._L.pcisph_batch_scene_stats(self._h, int(sid), C.byref(s)))
         return s
 
+    def graph_stats(self):
+        """(step graphs instantiated, updated in place) since creation."""
+        a, b = C.c_uint64(), C.c_uint64()
+        check(self._L.pcisph_batch_graph_stats(self._h, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
     def kernel_launches(self):
         return int(self._L.pcisph_batch_kernel_launches(self._h))
 

@@ -70,5 +70,25 @@ def build(force=False, verbose=False):
     return LIB
 
 
+CLI_SRC = os.path.join(PKG, "cli", "pcisph_run.cpp")
+CLI = os.path.join(PKG, "pcisph_run")
+
+
+def build_cli(force=False):
+    """The headless C++ runner (cli/pcisph_run.cpp) against the library; returns its path."""
+    lib = build()
+    deps = [CLI_SRC, lib, os.path.join(ROOT, "include", "pcisph_fluid.hpp"), os.path.join(ROOT, "include", "pcisph_gpu.h")]
+    if not force and not _stale(CLI, deps):
+        return CLI
+    cxx = shutil.which("g++") or "g++"
+    cmd = [cxx, "-std=c++17", "-O2", "-ffp-contract=off", "-I", os.path.join(ROOT, "include"), CLI_SRC, "-o", CLI + ".tmp", "-L", PKG,
+           "-l:libpcisph_gb300.so", "-Wl,-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"g++ failed on the runner:\n{r.stdout}\n{r.stderr}")
+    os.replace(CLI + ".tmp", CLI)
+    return CLI
+
+
 if __name__ == "__main__":
     print(build(force=True, verbose=True))

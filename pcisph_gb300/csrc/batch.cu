@@ -72,6 +72,7 @@ struct pcisph_batch {
     bool dirty = false;  // scenes were added or removed since the tables were built
     cudaGraphExec_t graph_exec = nullptr;
     bool graph_valid = false;
+    uint64_t graph_instantiations = 0, graph_updates = 0;
     uint64_t host_launches = 0;
     int prefix_launches = 0, iter_launches = 3;
     uint32_t *sorted_keys = nullptr, *sorted_ids = nullptr;
@@ -259,15 +260,29 @@ struct pcisph_batch {
         return cudaGetLastError() == cudaSuccess ? nl : -1;
     }
 
-    int build_graph() {
-        if (graph_exec) {
-            cudaGraphExecDestroy(graph_exec);
-            graph_exec = nullptr;
-        }
+    // Capture the step into a new graph. An existing executable graph is updated in place when only kernel
+    // parameters changed (a change of composition: particle and scene counts, table contents) -- far
+    // cheaper than instantiating again; otherwise it is replaced.
+    int capture(cudaGraph_t* out) {
         cudaStream_t s = capture_stream;
         cudaGraph_t graph = nullptr;
         BTRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
         const int nl = record_prefix(s);
+        if (loop_mode == 2) {  // the corrective loop as one cooperative kernel after the prefix
+            const cudaError_t le = nl < 0 ? cudaSuccess
+                                          : launch_corrective_loop_scenes(scene_table(), list_buffers(), d_batch,
+                                                                          max_iters, s);
+            const cudaError_t ee = cudaStreamEndCapture(s, &graph);
+            if (nl < 0 || le != cudaSuccess || ee != cudaSuccess) {
+                if (graph) cudaGraphDestroy(graph);
+                return report_error(PCISPH_ERR_CUDA, std::string("graph capture of the persistent batch step failed: ") +
+                                                         cudaGetErrorString(le != cudaSuccess ? le : ee));
+            }
+            prefix_launches = nl + 1;
+            iter_launches = 0;
+            *out = graph;
+            return PCISPH_OK;
+        }
         cudaStreamCaptureStatus st;
         const cudaGraphNode_t* deps = nullptr;
         size_t ndeps = 0;
@@ -280,50 +295,60 @@ struct pcisph_batch {
                                                      cudaGetErrorString(e != cudaSuccess ? e : e2));
         }
         prefix_launches = nl;
-        if (loop_mode == 2) {  // the corrective loop as one cooperative kernel after the prefix
-            cudaGraph_t g2 = nullptr;
-            cudaGraphDestroy(graph);
-            BTRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-            const int nl2 = record_prefix(s);
-            const cudaError_t le = nl2 < 0 ? cudaSuccess
-                                           : launch_corrective_loop_scenes(scene_table(), list_buffers(), d_batch,
-                                                                           max_iters, s);
-            const cudaError_t ee = cudaStreamEndCapture(s, &g2);
-            if (nl2 < 0 || le != cudaSuccess || ee != cudaSuccess) {
-                if (g2) cudaGraphDestroy(g2);
-                return report_error(PCISPH_ERR_CUDA, std::string("graph capture of the persistent batch step failed: ") +
-                                                         cudaGetErrorString(le != cudaSuccess ? le : ee));
-            }
-            prefix_launches = nl2 + 1;
-            iter_launches = 0;
-            const cudaError_t ie = cudaGraphInstantiate(&graph_exec, g2, 0);
-            cudaGraphDestroy(g2);
-            if (ie != cudaSuccess) return report_error(PCISPH_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ie));
-            graph_valid = true;
-            return PCISPH_OK;
-        }
         iter_launches = 3;
         cudaGraphConditionalHandle handle;
-        BTRY(cudaGraphConditionalHandleCreate(&handle, graph, 1, cudaGraphCondAssignDefault));
         cudaGraphNodeParams cp{};
-        cp.type = cudaGraphNodeTypeConditional;
-        cp.conditional.handle = handle;
-        cp.conditional.type = cudaGraphCondTypeWhile;
-        cp.conditional.size = 1;
         cudaGraphNode_t loop_node;
-        BTRY(cudaGraphAddNode(&loop_node, graph, leaves.data(), nullptr, leaves.size(), &cp));
-        BTRY(cudaStreamBeginCaptureToGraph(s, cp.conditional.phGraph_out[0], nullptr, nullptr, 0,
-                                           cudaStreamCaptureModeThreadLocal));
+        e = cudaGraphConditionalHandleCreate(&handle, graph, 1, cudaGraphCondAssignDefault);
+        if (e == cudaSuccess) {
+            cp.type = cudaGraphNodeTypeConditional;
+            cp.conditional.handle = handle;
+            cp.conditional.type = cudaGraphCondTypeWhile;
+            cp.conditional.size = 1;
+            e = cudaGraphAddNode(&loop_node, graph, leaves.data(), nullptr, leaves.size(), &cp);
+        }
+        if (e == cudaSuccess)
+            e = cudaStreamBeginCaptureToGraph(s, cp.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                              cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) {
+            cudaGraphDestroy(graph);
+            return report_error(PCISPH_ERR_CUDA, std::string("graph loop node: ") + cudaGetErrorString(e));
+        }
         const SceneTable t = scene_table();
         const ListBuffers b = list_buffers();
         launch_pressure_scenes(t, b, s);
         launch_batch_decide(t, d_batch, max_iters, handle, true, s);
         launch_pressure_force_scenes(t, b, s);
         cudaGraph_t body = nullptr;
-        BTRY(cudaStreamEndCapture(s, &body));
-        e = cudaGraphInstantiate(&graph_exec, graph, 0);
+        e = cudaStreamEndCapture(s, &body);
+        if (e != cudaSuccess) {
+            cudaGraphDestroy(graph);
+            return report_error(PCISPH_ERR_CUDA, std::string("graph loop body: ") + cudaGetErrorString(e));
+        }
+        *out = graph;
+        return PCISPH_OK;
+    }
+
+    int build_graph() {
+        cudaGraph_t graph = nullptr;
+        int rc = capture(&graph);
+        if (rc) return rc;
+        if (graph_exec) {
+            cudaGraphExecUpdateResultInfo info{};
+            if (cudaGraphExecUpdate(graph_exec, graph, &info) == cudaSuccess) {
+                cudaGraphDestroy(graph);
+                graph_valid = true;
+                ++graph_updates;
+                return PCISPH_OK;
+            }
+            (void)cudaGetLastError();  // the update was refused: instantiate instead
+            cudaGraphExecDestroy(graph_exec);
+            graph_exec = nullptr;
+        }
+        const cudaError_t e = cudaGraphInstantiate(&graph_exec, graph, 0);
         cudaGraphDestroy(graph);
         if (e != cudaSuccess) return report_error(PCISPH_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+        ++graph_instantiations;
         graph_valid = true;
         return PCISPH_OK;
     }
@@ -572,6 +597,13 @@ int pcisph_batch_get_field(pcisph_batch* b, int32_t id, int field, void* dst, si
         BTRY(cudaMemcpyAsync(dst, src, need, kind, st));
     }
     if (memory == PCISPH_MEM_HOST) BTRY(cudaStreamSynchronize(st));
+    return PCISPH_OK;
+}
+
+int pcisph_batch_graph_stats(const pcisph_batch* b, uint64_t* instantiations, uint64_t* updates) {
+    if (!b) return report_error(PCISPH_ERR_INVALID_ARG, "batch is NULL");
+    if (instantiations) *instantiations = b->graph_instantiations;
+    if (updates) *updates = b->graph_updates;
     return PCISPH_OK;
 }
 

@@ -105,7 +105,11 @@ struct pcisph_ctx {
     }
     bool warp_sweeps() const { return opts.kernel_variant == 0; }
     bool list_sweeps() const { return opts.kernel_variant == 2; }
-    bool working_order() const { return list_sweeps() && opts.spatial_order != 0; }
+    // spatial_order 1: on; 2 (default): on from 131,072 particles, where its cost (~100 us of sorting and
+    // scanning per step) is below what it saves in the sweeps
+    bool working_order() const {
+        return list_sweeps() && (opts.spatial_order == 1 || (opts.spatial_order == 2 && params.fluid_count >= (1u << 17)));
+    }
     ListBuffers list_buffers() const {
         const bool w = working_order();
         return ListBuffers{b.pos, b.vel, b.pr4, b.normal, b.f_other, b.f_press, b.pred, b.pf4, b.state_pos,
@@ -132,8 +136,8 @@ struct pcisph_ctx {
         w_of_d = c.take<uint32_t>(n);
         range_scratch = c.take<uint32_t>(working_ranges_scratch((uint32_t)bk));
         xfer = c.take<float4>(n);
-        bucket_sorter.set_digit_bits(10);
-        const size_t sbytes = RadixSorter::scratch_bytes(bk, 10);
+        bucket_sorter.set_digit_bits(8);
+        const size_t sbytes = RadixSorter::scratch_bytes(bk, 8);
         if (bucket_sort_block.ensure(sbytes) != cudaSuccess)
             return fail(PCISPH_ERR_OOM, "device allocation of the bucket-sort scratch failed");
         bucket_sorter.set_scratch(bucket_sort_block.p, bucket_sort_block.cap);
@@ -158,7 +162,7 @@ struct pcisph_ctx {
         uint32_t *ok = nullptr, *order = nullptr;
         cudaError_t e = cudaSuccess;
         timed("bucket_sort", s, [&] {
-            e = bucket_sorter.sort(bucket_codes, bucket_ids, BK, 30, true, s, &ok, &order);
+            e = bucket_sorter.sort(bucket_codes, bucket_ids, BK, 24, true, s, &ok, &order);
             nl += bucket_sorter.last_launches();
         });
         if (e != cudaSuccess) return -1;
@@ -873,7 +877,7 @@ int pcisph_default_options(pcisph_options* o) {
     o->loop_mode = 0;
     o->kernel_variant = 2;
     o->list_skin = 0.25f;
-    o->spatial_order = 1;
+    o->spatial_order = 2;
     return PCISPH_OK;
 }
 
@@ -1230,6 +1234,7 @@ int pcisph_autotune(pcisph_ctx* ctx, uint32_t steps, pcisph_tune_result* out) {
     const uint64_t launches0 = ctx->host_launches, steps0 = ctx->steps_launched, iters0 = ctx->host_mode_iters;
     const pcisph_options entry = ctx->opts;
     const int entry_bits = ctx->sorter.digit_bits();
+    const int entry_order = ctx->working_order() ? 1 : 0;  // "auto" as it resolves for this scene
     cudaEvent_t e0, e1;
     CUDA_TRY(cudaEventCreate(&e0));
     CUDA_TRY(cudaEventCreate(&e1));
@@ -1268,10 +1273,10 @@ int pcisph_autotune(pcisph_ctx* ctx, uint32_t steps, pcisph_tune_result* out) {
         return PCISPH_OK;
     };
     float before = 0.f;
-    rc = apply(entry.list_skin, entry.spatial_order, entry_bits);
+    rc = apply(entry.list_skin, entry_order, entry_bits);
     if (!rc) rc = time_it(&before);
     float best_ms = before, best_skin = entry.list_skin;
-    int best_order = entry.spatial_order, best_bits = entry_bits, n = 1;
+    int best_order = entry_order, best_bits = entry_bits, n = 1;
     const float skins[] = {0.15f, 0.2f, 0.25f, 0.3f};
     const int orders[] = {1, 0};
     const int bits[] = {8, 6};
@@ -1279,7 +1284,7 @@ int pcisph_autotune(pcisph_ctx* ctx, uint32_t steps, pcisph_tune_result* out) {
         for (int od : orders)
             for (int bt : bits) {
                 if (rc) break;
-                if (sk == entry.list_skin && od == entry.spatial_order && bt == entry_bits) continue;
+                if (sk == entry.list_skin && od == entry_order && bt == entry_bits) continue;
                 float ms = 0.f;
                 rc = apply(sk, od, bt);
                 if (!rc) rc = time_it(&ms);

@@ -183,8 +183,8 @@ __global__ void __launch_bounds__(kBlock) k_density_list(PS ps, ListBuffers b) {
     __shared__ uint32_t staged[2][8 * kBlock];  // current chunk of each thread's skin and within-h lists
     uint32_t* fbuf = staged[0];
     uint32_t* nbuf = staged[1];
-    for_each_neighbour(b.cells, c, P, [&](uint32_t j) {
-        const float4 o = __ldg(&b.pos[j]);
+    auto load = [&](uint32_t j) { return __ldg(&b.pos[j]); };
+    auto use = [&](uint32_t j, const float4& o) {
         const float dx = xi.x - o.x, dy = xi.y - o.y, dz = xi.z - o.z;
         const float r2 = dist2(dx, dy, dz);
         acc += poly6(r2, P.h2);
@@ -196,7 +196,8 @@ __global__ void __launch_bounds__(kBlock) k_density_list(PS ps, ListBuffers b) {
                 ++nn;
             }
         }
-    });
+    };
+    for_each_neighbour_prefetched(b.cells, c, P, load, use);
     list_finish(b.nbr, i, stride, fbuf, n, P.list_cap);
     list_finish(b.near, i, stride, nbuf, nn, P.near_cap);
     b.nbr_count[i] = n;  // n > list_cap: this particle walks the buckets in the pressure sweeps

@@ -9,9 +9,9 @@ constexpr int kRounds = 16;                     // elements per thread in the ra
 constexpr int kScanTile = kBlock * kRounds;     // elements per block
 inline unsigned grid_for(uint32_t n) { return (n + kBlock - 1) / kBlock; }
 
-// 10 low bits of v spread to every third bit (bit k -> bit 3k)
+// 8 low bits of v spread to every third bit (bit k -> bit 3k)
 __device__ __forceinline__ uint32_t spread3(uint32_t v) {
-    v &= 0x3FFu;
+    v &= 0xFFu;
     v = (v | (v << 16)) & 0x030000FFu;
     v = (v | (v << 8)) & 0x0300F00Fu;
     v = (v | (v << 4)) & 0x030C30C3u;

@@ -16,7 +16,7 @@
 namespace pcisph {
 
 // Per bucket: cells_d[key] = its range in sorted order (the reference's table, reorder semantics);
-// codes[key] = Morton code (10 bits per axis) of its first particle's cell, all ones when empty (the
+// codes[key] = Morton code (8 bits per axis, 24 bits) of its first particle's cell, all ones when empty (the
 // caller fills codes with 0xFF bytes first). Out-of-range sorted entries set status bit 4.
 void launch_bucket_codes(const uint32_t* sorted_keys, const uint32_t* sorted_ids, const float4* state_pos,
                          uint32_t n, const DevParams& P, uint2* cells_d, uint32_t* codes, Control* ctl,

@@ -265,7 +265,7 @@ class Fluid:
 
 
 def setup_scene(fluid, scene, walls=None, loop_mode=0, max_iters=None, min_iters=None, boundary_self_density=0,
-                kernel_variant=2, spatial_order=1):
+                kernel_variant=2, spatial_order=2):
     """Configure ``fluid`` for a scenes.Scene the way scene::load does (scenes.cpp:217-245)."""
     fluid.set_delta_t(scene.delta_t)
     fluid.set_rest_density(scene.rest_density)

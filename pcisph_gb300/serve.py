@@ -20,16 +20,41 @@ import numpy as np
 from . import scenes as _scenes
 
 
-@dataclass
 class Request:
-    rid: int
-    arrival: float      # seconds after the start of the run
-    scene: object       # scenes.Scene
-    steps: int          # rollout length (time steps)
+    """A rollout request: `steps` time steps of a scene. The scene is given, or built on first use from a
+    spec (kind, target particle count, aspect ratios, seed, jitter id offset), so a long queue of requests
+    holds no particle arrays."""
+
+    def __init__(self, rid, arrival, scene=None, steps=0, spec=None):
+        self.rid, self.arrival, self.steps, self.spec = rid, float(arrival), int(steps), spec
+        self._scene = scene
+
+    @property
+    def scene(self):
+        if self._scene is None:
+            kind, n, ax, az, seed, offset, d, dt = self.spec
+            if kind == "dam":
+                self._scene = _scenes.batch_dam(n, ax, az, d, seed, offset, dt, f"req{self.rid}")
+            else:
+                self._scene = _scenes.batch_drop(n, d, seed, offset, dt, name=f"req{self.rid}")
+        return self._scene
+
+    def release(self):
+        """Drop a built scene's arrays (it is rebuilt, identically, if used again)."""
+        if self.spec is not None:
+            self._scene = None
 
     @property
     def particles(self):
         return self.scene.fluid_count
+
+    @property
+    def particles_bound(self):
+        """An upper bound of the particle count that needs no scene (the generators stay within 20% of
+        their target count; the bound allows 30%)."""
+        if self.spec is None:
+            return self.particles
+        return int(1.3 * self.spec[1]) + 256
 
 
 @dataclass
@@ -58,25 +83,18 @@ def poisson_requests(count, rate, n_min=2048, n_max=262144, steps_min=100, steps
                      delta_t=1e-3):
     """The serving workload: `count` requests with exponential inter-arrival times at `rate` per second,
     particle counts log-uniform in [n_min, n_max], rollouts uniform in [steps_min, steps_max]; scenes as
-    the batched workload (dam-break blocks or spheres dropped into a pool). Deterministic in `seed`."""
+    the batched workload (dam-break blocks or spheres dropped into a pool), built when first used; request
+    k's particles draw their jitter from ids k * 2^20 + i. Deterministic in `seed`."""
     ids = np.arange(count, dtype=np.uint64)
-    u_t = _scenes.uniform(seed, ids, 0, stream=2)
-    u_n = _scenes.uniform(seed, ids, 1, stream=2)
-    u_r = _scenes.uniform(seed, ids, 2, stream=2)
-    u_k = _scenes.uniform(seed, ids, 3, stream=2)
-    u_a = _scenes.uniform(seed, ids, 4, stream=2)
-    u_b = _scenes.uniform(seed, ids, 5, stream=2)
+    u_t, u_n, u_r, u_k, u_a, u_b = (_scenes.uniform(seed, ids, a, stream=2) for a in range(6))
     arrivals = np.cumsum(-np.log1p(-u_t) / rate)
-    out, offset = [], 0
+    out = []
     for k in range(count):
         n = int(round(math.exp(math.log(n_min) + u_n[k] * (math.log(n_max) - math.log(n_min)))))
         steps = steps_min + int(u_r[k] * (steps_max - steps_min + 1))
-        if u_k[k] < 0.5:
-            sc = _scenes.batch_dam(n, 0.5 + 1.5 * u_a[k], 0.5 + 1.5 * u_b[k], d, seed, offset, delta_t, f"req{k}")
-        else:
-            sc = _scenes.batch_drop(n, d, seed, offset, delta_t, name=f"req{k}")
-        offset += sc.fluid_count
-        out.append(Request(k, float(arrivals[k]), sc, steps))
+        kind = "dam" if u_k[k] < 0.5 else "drop"
+        spec = (kind, n, 0.5 + 1.5 * float(u_a[k]), 0.5 + 1.5 * float(u_b[k]), seed, k << 20, d, delta_t)
+        out.append(Request(k, float(arrivals[k]), steps=steps, spec=spec))
     return out
 
 
@@ -147,12 +165,15 @@ class Server:
         self.running = []        # _Running, admission order
         self.used_bytes = 0
         self.used_particles = 0
+        self._particles = {}     # particle count of every admitted request
 
     def cost(self, req):
-        return req.particles * self.bpp + self.bps
+        n = self._particles.get(req.rid)
+        return (req.particles if n is None else n) * self.bpp + self.bps
 
     def fits_ever(self, req):
-        return self.cost(req) <= self.budget and req.particles <= self.max_particles
+        n = req.particles_bound  # at arrival: no scene is built for a request that may wait long
+        return n * self.bpp + self.bps <= self.budget and n <= self.max_particles
 
     def _admit(self, now):
         admitted = 0
@@ -167,6 +188,8 @@ class Server:
             self.running.append(_Running(req, sid, arrived, now, req.steps))
             self.used_bytes += self.cost(req)
             self.used_particles += req.particles
+            self._particles[req.rid] = req.particles
+            req.release()  # the pool holds the state now
             admitted += 1
         return admitted
 
@@ -179,13 +202,15 @@ class Server:
             st = self.batch.stats(r.sid)
             pos = vel = None
             if self.keep_state:
-                pos = self.batch.get_field(r.sid, "position", r.req.particles)
-                vel = self.batch.get_field(r.sid, "velocity", r.req.particles)
+                n = self._particles[r.req.rid]
+                pos = self.batch.get_field(r.sid, "position", n)
+                vel = self.batch.get_field(r.sid, "velocity", n)
             self.batch.remove_scene(r.sid)
-            self.used_bytes -= self.cost(r.req)
-            self.used_particles -= r.req.particles
+            n = self._particles.pop(r.req.rid)
+            self.used_bytes -= n * self.bpp + self.bps
+            self.used_particles -= n
             out.append(Completion(r.req.rid, r.arrived, r.admitted, self.clock_now(), r.req.steps,
-                                  r.req.particles, int(st.total_iterations), int(st.status_all), pos, vel))
+                                  n, int(st.total_iterations), int(st.status_all), pos, vel))
         self.running = keep
         return out
 

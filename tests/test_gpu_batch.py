@@ -83,6 +83,8 @@ def test_batch_remove_and_add_scenes():
         _assert_same(sc[k].name, _in_batch(bt, ids[k], sc[k]), _alone(sc[k], 9))
     _assert_same(sc[4].name, _in_batch(bt, e_id, sc[4]), _alone(sc[4], 4))
     assert bt.info()[0] == 4
+    inst, upd = bt.graph_stats()
+    assert inst == 1 and upd == 1  # the change of composition updated the step graph in place
 
 
 def test_batch_limits_and_errors():
