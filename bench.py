@@ -79,6 +79,23 @@ def parse():
     return ap.parse_args()
 
 
+def max_over_ranks(x):
+    """The largest of every rank's x (the timed region of the slowest rank); x itself on one rank."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(x)
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(units_per_rank, world, max_ms):
+    """Whole-job throughput of `world` replicas that each processed units_per_rank in at most max_ms."""
+    return units_per_rank * world / (max_ms / 1e3)
+
+
 def dist_env():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
 
@@ -194,7 +211,8 @@ def reference_arm(args, rank, world):
         "unit": "particle-steps/s", "n_gpus": 0, "steps": steps, "warmup": w, "ms_per_step": 1e3 * sc.fluid_count / rate,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded jittered lattice)",
-        "config": {"workload": workload, "particles": sc.fluid_count, "mean_iterations": iters},
+        "config": {"workload": workload, "particles": sc.fluid_count, "mean_iterations": iters,
+                   "particle_iterations_per_s": rate * iters},
         "cpu_baseline": {"value": rate, "unit": "particle-steps/s", "cores": cores, "kind": "port",
                          "sample": f"{sc.fluid_count} particles x {steps} steps after {w} warm-up steps "
                                    f"(oracle/pcisph_oracle.cpp, OpenMP over particles; the reference's OpenCL "
@@ -237,12 +255,7 @@ def scenes_workload(args, rank, world, local):
             step_fn()
             ends[k].record(stream)
         torch.cuda.synchronize()
-        ms = sum(a.elapsed_time(b) for a, b in zip(starts, ends))
-        if world > 1:
-            t = torch.tensor([ms], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = float(t.item())
-        return ms
+        return max_over_ranks(sum(a.elapsed_time(b) for a, b in zip(starts, ends)))
 
     # batched: every scene in one pool, one graph launch per step
     bt = Batch(local, max_particles=n_total, max_scenes=len(sc), stream=stream.cuda_stream, loop_mode=args.loop_mode)
@@ -462,14 +475,10 @@ def main():
     st1 = f.stats()
     launches = f.kernel_launches() - launches0
     step_ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
-    total_ms = sum(step_ms)
-    if world > 1:
-        t = torch.tensor([total_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = max_over_ranks(sum(step_ms))
     iters = (st1.total_iterations - st0.total_iterations) / max(1, st1.steps - st0.steps)
     status_bits = st1.status_all
-    value = N * args.steps * world / (total_ms / 1e3)
+    value = replica_value(N * args.steps, world, total_ms)
 
     # per-kernel CUDA events over the first steps of the timed loop again (host-driven loop, same kernels)
     prof_steps = min(args.steps, 20)
@@ -519,7 +528,8 @@ def main():
         rate, csteps, citers, _ = cpu_step_rate(sc, start_pos, start_vel, args.cpu_seconds, max_steps=args.steps)
         cpu = {"value": rate, "unit": "particle-steps/s", "cores": os.cpu_count(), "kind": "port",
                "sample": f"{N} particles x the first {csteps} of the timed steps, from the same state "
-                         f"(mean {citers:.2f} corrective iterations), oracle/pcisph_oracle.cpp with OpenMP"}
+                         f"(mean {citers:.2f} corrective iterations), oracle/pcisph_oracle.cpp with OpenMP",
+               "mean_iterations": citers, "particle_iterations_per_s": rate * citers}
     if rank == 0:
         line = {
             "metric": metric, "value": value, "unit": "particle-steps/s",
@@ -528,7 +538,8 @@ def main():
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded jittered lattice)",
             "config": {"workload": workload, "particles": N, "parallelism": f"replicas x{world}",
                        "kernel_variant": args.variant, "loop_mode": args.loop_mode,
-                       "mean_iterations": iters, "max_density_error_last": st1.max_density_error,
+                       "mean_iterations": iters, "particle_iterations_per_s": value * iters,
+                       "max_density_error_last": st1.max_density_error,
                        "step_ms_min_median_max": [min(step_ms), statistics.median(step_ms), max(step_ms)],
                        "converged_all_steps": (status_bits & 1) == 0, "status_bits": status_bits,
                        "l2": "256 MB written between timed steps (not timed); step working set ~200 MB > L2",
