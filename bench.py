@@ -74,6 +74,8 @@ def parse():
     ap.add_argument("--budget-gb", type=float, default=100.0, help="device memory budget of --workload serve")
     ap.add_argument("--duration", type=float, default=120.0, help="wall-time bound (s) of --workload serve")
     ap.add_argument("--scenes", type=int, default=256, help="scene count of --workload scenes")
+    ap.add_argument("--autotune", action="store_true",
+                    help="run the library's autotuner on the warmed-up state before timing (results unchanged)")
     ap.add_argument("--loop-mode", type=int, default=0, choices=[0, 2],
                     help="corrective loop: 0 graph WHILE node, 2 persistent cooperative kernel")
     return ap.parse_args()
@@ -263,6 +265,7 @@ def scenes_workload(args, rank, world, local):
     for _ in range(args.warmup):
         bt.step(1)
     bt.sync()
+    tuned = bt.autotune(steps=2) if args.autotune else None
     snap = [(bt.get_field(i, "position", s.fluid_count), bt.get_field(i, "velocity", s.fluid_count))
             for i, s in zip(ids, sc)]
     st0 = [bt.stats(i) for i in ids]
@@ -333,7 +336,7 @@ def scenes_workload(args, rank, world, local):
                        "parallelism": f"scenes sharded over {world} GPU(s)",
                        "scene_steps_per_s": len(all_sc) * args.steps / (ms_batch / 1e3),
                        "mean_scene_iterations": float(np.mean(iters)), "batch_loop_iterations": batch_loop_iters,
-                       "loop_mode": args.loop_mode,
+                       "loop_mode": args.loop_mode, "autotuned": tuned,
                        "l2": "working set ~6 GB > L2"},
             "per_scene_contexts": {"value": n_all * args.steps / (ms_single / 1e3), "unit": "particle-steps/s",
                                    "ms_per_step": ms_single / args.steps, "gpu_launches": single_launches,
@@ -446,6 +449,7 @@ def main():
     for _ in range(args.warmup):
         f.update()
     torch.cuda.synchronize()
+    tuned = f.autotune(steps=3) if args.autotune else None
     # snapshot of the state after warm-up: the profile pass, the e2e pass and the CPU baseline replay the
     # same steps as the timed loop (the step is deterministic)
     snap_pos = torch.empty((N, 4), dtype=torch.float32, device="cuda")
@@ -537,7 +541,7 @@ def main():
             "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded jittered lattice)",
             "config": {"workload": workload, "particles": N, "parallelism": f"replicas x{world}",
-                       "kernel_variant": args.variant, "loop_mode": args.loop_mode,
+                       "kernel_variant": args.variant, "loop_mode": args.loop_mode, "autotuned": tuned,
                        "mean_iterations": iters, "particle_iterations_per_s": value * iters,
                        "max_density_error_last": st1.max_density_error,
                        "step_ms_min_median_max": [min(step_ms), statistics.median(step_ms), max(step_ms)],

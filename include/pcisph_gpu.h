@@ -297,6 +297,18 @@ PCISPH_API int pcisph_batch_add_scene(pcisph_batch* batch, const pcisph_scene_de
 /* Removes a scene: its id is invalid at once; its particles leave the pool at the next step, which compacts
  * the pool once for all removals (stream-ordered device copies). */
 PCISPH_API int pcisph_batch_remove_scene(pcisph_batch* batch, int32_t scene_id);
+/* Autotuning of a batch on its current scenes: times `steps` batched steps (after a warm-up step) for each
+ * list skin 0.2, 0.25, 0.3 x loop mode 0, 2 x radix digit width 8, 6, restoring the pool's state and
+ * statistics after each, and keeps the fastest. Every candidate computes the same bits. Synchronises. */
+typedef struct pcisph_batch_tune_result {
+    float list_skin;
+    int32_t loop_mode;
+    int32_t digit_bits;
+    float ms_per_step;
+    float ms_per_step_before;
+    int32_t candidates;
+} pcisph_batch_tune_result;
+PCISPH_API int pcisph_batch_autotune(pcisph_batch* batch, uint32_t steps, pcisph_batch_tune_result* out);
 /* 0 (default): the corrective loop is a conditional WHILE node of the step's graph; 2: one persistent
  * cooperative kernel runs it with per-scene convergence flags. Same results either way. */
 PCISPH_API int pcisph_batch_set_loop_mode(pcisph_batch* batch, int loop_mode);

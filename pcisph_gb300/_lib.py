@@ -78,6 +78,11 @@ class TuneResult(C.Structure):
                 ("ms_per_step", C.c_float), ("ms_per_step_before", C.c_float), ("candidates", C.c_int32)]
 
 
+class BatchTuneResult(C.Structure):
+    _fields_ = [("list_skin", C.c_float), ("loop_mode", C.c_int32), ("digit_bits", C.c_int32),
+                ("ms_per_step", C.c_float), ("ms_per_step_before", C.c_float), ("candidates", C.c_int32)]
+
+
 class KernelTime(C.Structure):
     _fields_ = [("name", C.c_char * 32), ("launches", C.c_uint64), ("total_ms", C.c_double)]
 
@@ -170,6 +175,7 @@ def load():
         "pcisph_batch_get_field": ([vp, C.c_int32, i32, vp, sz, i32, i32], i32),
         "pcisph_batch_set_state": ([vp, C.c_int32, vp, vp, C.c_uint32, i32, i32], i32),
         "pcisph_batch_set_loop_mode": ([vp, i32], i32),
+        "pcisph_batch_autotune": ([vp, C.c_uint32, C.POINTER(BatchTuneResult)], i32),
         "pcisph_batch_graph_stats": ([vp, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)], i32),
         "pcisph_batch_kernel_launches": ([vp], C.c_uint64),
     }

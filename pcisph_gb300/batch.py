@@ -83,6 +83,15 @@ class Batch:
                                              None if vel is None else C.c_void_p(vel.ctypes.data),
                                              pos.shape[0], layout, _lib.MEM_HOST))
 
+    def autotune(self, steps=2):
+        """Pick the fastest list skin / loop mode / sort digit width on the current scenes (results are
+        unchanged by any choice); returns the choice and the step times."""
+        r = _lib.BatchTuneResult()
+        check(self._L.pcisph_batch_autotune(self._h, int(steps), C.byref(r)))
+        return {"list_skin": r.list_skin, "loop_mode": r.loop_mode, "digit_bits": r.digit_bits,
+                "ms_per_step": r.ms_per_step, "ms_per_step_before": r.ms_per_step_before,
+                "candidates": r.candidates}
+
     def set_loop_mode(self, mode):
         """0: the corrective loop as a graph WHILE node; 2: one persistent cooperative kernel."""
         check(self._L.pcisph_batch_set_loop_mode(self._h, int(mode)))

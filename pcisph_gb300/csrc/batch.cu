@@ -69,6 +69,7 @@ struct pcisph_batch {
     uint32_t n_particles = 0, n_buckets = 0;
     int max_iters = 1;
     int loop_mode = 0;   // 0: conditional WHILE node; 2: one persistent cooperative kernel
+    float list_skin = 0.25f;
     bool dirty = false;  // scenes were added or removed since the tables were built
     cudaGraphExec_t graph_exec = nullptr;
     bool graph_valid = false;
@@ -212,7 +213,7 @@ struct pcisph_batch {
             s.bucket_base = base;
             const pcisph_scene_desc& d = s.desc;
             make_devparams(s.params, d.min_iterations, d.max_iterations, d.walls, d.box_lo, d.box_hi, d.restitution,
-                           d.density_variation_threshold, 0.25f, base, &table[k]);
+                           d.density_variation_threshold, list_skin, base, &table[k]);
             offsets[k] = off;
             off += s.count;
             base += s.params.bucket_count;
@@ -502,6 +503,107 @@ int pcisph_batch_remove_scene(pcisph_batch* b, int32_t id) {
     if (k < 0) return report_error(PCISPH_ERR_INVALID_ARG, "unknown scene id " + std::to_string(id));
     b->scenes[k].removed = true;  // compacted with every other removal at the next step
     b->dirty = true;
+    return PCISPH_OK;
+}
+
+int pcisph_batch_autotune(pcisph_batch* b, uint32_t steps, pcisph_batch_tune_result* out) {
+    if (!b || !out) return report_error(PCISPH_ERR_INVALID_ARG, "NULL argument");
+    if (steps == 0 || steps > 1000) return report_error(PCISPH_ERR_INVALID_ARG, "steps must be in 1..1000");
+    DeviceGuard g(b->device);
+    if (b->dirty) {
+        int rc = b->compact();
+        if (rc) return rc;
+    }
+    const uint32_t n = b->n_particles, ns = (uint32_t)b->scenes.size();
+    if (n == 0) return report_error(PCISPH_ERR_NOT_READY, "no scenes to tune on");
+    cudaStream_t s = b->stream();
+    DeviceBlock saved;
+    if (saved.ensure((size_t)n * 32 + (size_t)ns * sizeof(Control) + sizeof(Control)) != cudaSuccess)
+        return report_error(PCISPH_ERR_OOM, "device allocation for autotuning failed");
+    float4* sp = static_cast<float4*>(saved.p);
+    Control* sc = reinterpret_cast<Control*>(sp + 2 * (size_t)n);
+    BTRY(cudaMemcpyAsync(sp, b->state_pos, (size_t)n * 16, cudaMemcpyDeviceToDevice, s));
+    BTRY(cudaMemcpyAsync(sp + n, b->state_vel, (size_t)n * 16, cudaMemcpyDeviceToDevice, s));
+    BTRY(cudaMemcpyAsync(sc, b->d_ctls, (size_t)ns * sizeof(Control), cudaMemcpyDeviceToDevice, s));
+    BTRY(cudaMemcpyAsync(sc + ns, b->d_batch, sizeof(Control), cudaMemcpyDeviceToDevice, s));
+    const uint64_t launches0 = b->host_launches;
+    const float entry_skin = b->list_skin;
+    const int entry_mode = b->loop_mode, entry_bits = b->sorter.digit_bits();
+    auto restore = [&]() -> int {
+        BTRY(cudaMemcpyAsync(b->state_pos, sp, (size_t)n * 16, cudaMemcpyDeviceToDevice, s));
+        BTRY(cudaMemcpyAsync(b->state_vel, sp + n, (size_t)n * 16, cudaMemcpyDeviceToDevice, s));
+        BTRY(cudaMemcpyAsync(b->d_ctls, sc, (size_t)ns * sizeof(Control), cudaMemcpyDeviceToDevice, s));
+        BTRY(cudaMemcpyAsync(b->d_batch, sc + ns, sizeof(Control), cudaMemcpyDeviceToDevice, s));
+        BTRY(cudaStreamSynchronize(s));
+        return PCISPH_OK;
+    };
+    auto apply = [&](float skin, int mode, int bits) -> int {
+        b->list_skin = skin;
+        b->loop_mode = mode;
+        b->sorter.set_digit_bits(bits);
+        b->sort_block.release();
+        const size_t sbytes = RadixSorter::scratch_bytes(b->max_particles, bits);
+        if (b->sort_block.ensure(sbytes) != cudaSuccess)
+            return report_error(PCISPH_ERR_OOM, "device allocation of the sort scratch failed");
+        b->sorter.set_scratch(b->sort_block.p, b->sort_block.cap);
+        b->graph_valid = false;
+        return b->rebuild();  // scene tables with the new skin
+    };
+    cudaEvent_t e0, e1;
+    BTRY(cudaEventCreate(&e0));
+    BTRY(cudaEventCreate(&e1));
+    auto time_it = [&](float* ms) -> int {
+        int r = restore();
+        if (!r) r = b->step(1);  // warm-up: builds the graph
+        if (!r) r = restore();
+        if (r) return r;
+        BTRY(cudaEventRecord(e0, s));
+        r = b->step(steps);
+        BTRY(cudaEventRecord(e1, s));
+        BTRY(cudaEventSynchronize(e1));
+        if (r) return r;
+        BTRY(cudaEventElapsedTime(ms, e0, e1));
+        *ms /= (float)steps;
+        return PCISPH_OK;
+    };
+    float before = 0.f;
+    int rc = apply(entry_skin, entry_mode, entry_bits);
+    if (!rc) rc = time_it(&before);
+    float best_ms = before, best_skin = entry_skin;
+    int best_mode = entry_mode, best_bits = entry_bits, cands = 1;
+    const float skins[] = {0.2f, 0.25f, 0.3f};
+    const int modes[] = {0, 2};
+    const int bits[] = {8, 6};
+    for (float sk : skins)
+        for (int md : modes)
+            for (int bt : bits) {
+                if (rc) break;
+                if (sk == entry_skin && md == entry_mode && bt == entry_bits) continue;
+                float ms = 0.f;
+                rc = apply(sk, md, bt);
+                if (!rc) rc = time_it(&ms);
+                ++cands;
+                if (!rc && ms < best_ms) {
+                    best_ms = ms;
+                    best_skin = sk;
+                    best_mode = md;
+                    best_bits = bt;
+                }
+            }
+    if (!rc) rc = apply(best_skin, best_mode, best_bits);
+    const int rc2 = restore();
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    saved.release();
+    b->host_launches = launches0;
+    if (rc) return rc;
+    if (rc2) return rc2;
+    out->list_skin = best_skin;
+    out->loop_mode = best_mode;
+    out->digit_bits = best_bits;
+    out->ms_per_step = best_ms;
+    out->ms_per_step_before = before;
+    out->candidates = cands;
     return PCISPH_OK;
 }
 

@@ -145,3 +145,21 @@ def test_persistent_loop_batch_matches_graph_loop():
         bt.close()
     for s, a, b in zip(sc, out[0], out[1]):
         _assert_same(s.name, b, a)
+
+
+def test_batch_autotune_leaves_results_unchanged():
+    sc = _mixed_scenes()
+    out = []
+    for tune in (False, True):
+        bt = Batch(0, max_particles=sum(s.fluid_count for s in sc), max_scenes=len(sc))
+        ids = [bt.add_scene(s) for s in sc]
+        bt.step(2)
+        if tune:
+            r = bt.autotune(steps=1)
+            assert r["candidates"] == 12 and r["ms_per_step"] <= r["ms_per_step_before"]
+        bt.step(4)
+        bt.sync()
+        out.append([_in_batch(bt, i, s) for i, s in zip(ids, sc)])
+        bt.close()
+    for s, a, b in zip(sc, out[0], out[1]):
+        _assert_same(s.name, b, a)
