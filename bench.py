@@ -42,6 +42,11 @@ ALGO_BYTES = {
     "hash": 20,             # x 12 + key 4 + id 4
     "radix_sort": 48,       # 3 passes of 8 B read + 8 B written
 }
+# compulsory bytes of a whole step per particle: 340 + 136 per corrective iteration (hash 20, 3 sort passes
+# 60, cell reset 4, reorder 60, density 20, normal 32, force 72, integrate 72; per iteration predict 60,
+# pressure 40, pressure force 36), vectors at their 12-byte payload
+STEP_FIXED_BYTES = 340
+STEP_ITER_BYTES = 136
 DAM_WORKLOADS = {
     "dam1m": ("config1", "particle-steps/s @1M (<=1% rho err)",
               "dam break 128x128x64 = 1,048,576 particles, d=0.005 m, dt=2.5e-4 s, reflecting walls, "
@@ -169,6 +174,29 @@ class ClockSampler:
         return {"sm_mhz": statistics.median(sm) if sm else None,
                 "sm_max_mhz": float(rows[0][2]) if rows[0][2].replace(".", "").isdigit() else None,
                 "reasons": reasons, "samples": len(rows)}
+
+
+def walk_candidates(f):
+    """Mean candidates per particle of the reference's 27-bucket walk (grid_utils.cl:65-79) at the last
+    step's sorted positions: the pair evaluations each of its neighbour sweeps makes per particle."""
+    import numpy as np
+    p = f.get_params()
+    pos = f.get_field("sorted_position").astype(np.float32)
+    off = f.get_field("cell_offsets").reshape(-1, 2).astype(np.int64)
+    lens = np.maximum(off[:, 1] - off[:, 0], 0)
+    bk = np.uint64(p.bucket_count)
+    cell = np.floor(pos / np.float32(p.cell_size)).clip(-2.0 ** 31, 2.0 ** 31 - 1).astype(np.int64)
+    total = np.zeros(pos.shape[0], np.int64)
+    m32 = np.int64(0xFFFFFFFF)
+    for k in range(27):
+        x = (cell[:, 0] + (k % 3 - 1)) & m32
+        y = (cell[:, 1] + ((k // 3) % 3 - 1)) & m32
+        z = (cell[:, 2] + (k // 9 - 1)) & m32
+        h = ((x * 19349663) & m32) ^ ((y * 73856093) & m32) ^ ((z * 83492791) & m32)
+        v = (((h << 6) & m32) + (x & 63) + 4 * (y & 63) + 16 * (z & 63)) & m32
+        key = ((v & 0x7FFFFFFF).astype(np.uint64) % bk).astype(np.int64)
+        total += lens[key]
+    return float(total.mean()) if total.size else 0.0
 
 
 def cpu_step_rate(scene, pos, vel, seconds, max_steps=None):
@@ -527,6 +555,8 @@ def main():
            "d2h_bytes_per_step": 24 * N, "steps": e2e_steps,
            "device_value_same_steps": N * e2e_steps * world / (sum(step_ms[:e2e_steps]) / 1e3)}
 
+    cand = walk_candidates(f)
+    step_bytes = STEP_FIXED_BYTES + STEP_ITER_BYTES * iters
     cpu = None
     if rank == 0 and world == 1:
         rate, csteps, citers, _ = cpu_step_rate(sc, start_pos, start_vel, args.cpu_seconds, max_steps=args.steps)
@@ -547,7 +577,11 @@ def main():
                        "step_ms_min_median_max": [min(step_ms), statistics.median(step_ms), max(step_ms)],
                        "converged_all_steps": (status_bits & 1) == 0, "status_bits": status_bits,
                        "l2": "256 MB written between timed steps (not timed); step working set ~200 MB > L2",
-                       "wall_s_timed_loop": wall},
+                       "wall_s_timed_loop": wall,
+                       "step_algorithmic_bytes_per_particle": step_bytes,
+                       "step_hbm_frac": step_bytes * value / (peak * 1e9),
+                       "walk_candidates_per_particle": cand,
+                       "reference_pair_evaluations_per_s": cand * (3 + 2 * iters) * value},
             "e2e": e2e,
             "gpu_launches": launches,
             "roofline": {"bound": "hbm", "kernel": dname, "achieved": achieved, "peak": peak, "unit": "GB/s",
