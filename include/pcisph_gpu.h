@@ -208,6 +208,10 @@ PCISPH_API int pcisph_check_buffers_consistent(const pcisph_ctx* ctx);
 PCISPH_API int pcisph_update(pcisph_ctx* ctx);
 PCISPH_API int pcisph_step(pcisph_ctx* ctx, uint32_t steps);
 PCISPH_API int pcisph_sync(pcisph_ctx* ctx);
+/* Bounded wait: PCISPH_ERR_TIMEOUT if the queued work is still running after timeout_ms (0: query once).
+ * Nothing is cancelled; a later sync picks the work up. For callers that must not block (a serving loop
+ * watching for stalled steps). */
+PCISPH_API int pcisph_sync_for(pcisph_ctx* ctx, int64_t timeout_ms);
 /* Synchronises, then reports the last step. */
 PCISPH_API int pcisph_last_stats(pcisph_ctx* ctx, pcisph_step_stats* out);
 PCISPH_API int pcisph_reset_stats(pcisph_ctx* ctx);
@@ -317,6 +321,8 @@ PCISPH_API int pcisph_batch_info(const pcisph_batch* batch, uint32_t* scenes, ui
 /* steps time steps of every scene (one CUDA graph launch each; no host synchronisation). */
 PCISPH_API int pcisph_batch_step(pcisph_batch* batch, uint32_t steps);
 PCISPH_API int pcisph_batch_sync(pcisph_batch* batch);
+/* pcisph_sync_for for a batch's stream. */
+PCISPH_API int pcisph_batch_sync_for(pcisph_batch* batch, int64_t timeout_ms);
 /* Synchronises, then reports the scene's last step (and totals since it was added). */
 PCISPH_API int pcisph_batch_scene_stats(pcisph_batch* batch, int32_t scene_id, pcisph_step_stats* out);
 /* Replaces a scene's positions (and velocities; NULL: zero), as pcisph_set_fluid_state; count must be the

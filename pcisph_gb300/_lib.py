@@ -141,6 +141,7 @@ def load():
         "pcisph_update": ([vp], i32),
         "pcisph_step": ([vp, u32], i32),
         "pcisph_sync": ([vp], i32),
+        "pcisph_sync_for": ([vp, C.c_int64], i32),
         "pcisph_last_stats": ([vp, C.POINTER(StepStats)], i32),
         "pcisph_reset_stats": ([vp], i32),
         "pcisph_get_field": ([vp, i32, vp, sz, i32, i32], i32),
@@ -171,6 +172,7 @@ def load():
         "pcisph_batch_info": ([vp, C.POINTER(u32), C.POINTER(u32), C.POINTER(u32)], i32),
         "pcisph_batch_step": ([vp, u32], i32),
         "pcisph_batch_sync": ([vp], i32),
+        "pcisph_batch_sync_for": ([vp, C.c_int64], i32),
         "pcisph_batch_scene_stats": ([vp, C.c_int32, C.POINTER(StepStats)], i32),
         "pcisph_batch_get_field": ([vp, C.c_int32, i32, vp, sz, i32, i32], i32),
         "pcisph_batch_set_state": ([vp, C.c_int32, vp, vp, C.c_uint32, i32, i32], i32),

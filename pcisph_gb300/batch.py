@@ -107,8 +107,13 @@ class Batch:
     def step(self, n=1):
         check(self._L.pcisph_batch_step(self._h, int(n)))
 
-    def sync(self):
-        check(self._L.pcisph_batch_sync(self._h))
+    def sync(self, timeout_ms=None):
+        """Wait for the queued steps; with timeout_ms, raise PcisphError (ERR_TIMEOUT) if they are still
+        running after that many milliseconds (the work stays queued)."""
+        if timeout_ms is None:
+            check(self._L.pcisph_batch_sync(self._h))
+        else:
+            check(self._L.pcisph_batch_sync_for(self._h, int(timeout_ms)))
 
     def stats(self, sid):
         s = StepStats()

@@ -639,6 +639,17 @@ int pcisph_batch_sync(pcisph_batch* b) {
     return PCISPH_OK;
 }
 
+int pcisph_batch_sync_for(pcisph_batch* b, int64_t timeout_ms) {
+    if (!b) return report_error(PCISPH_ERR_INVALID_ARG, "batch is NULL");
+    if (timeout_ms < 0) return report_error(PCISPH_ERR_INVALID_ARG, "timeout_ms must be >= 0");
+    DeviceGuard g(b->device);
+    bool done = false;
+    BTRY(host::wait_stream_for(b->stream(), timeout_ms, &done));
+    if (!done)
+        return report_error(PCISPH_ERR_TIMEOUT, "queued steps still running after " + std::to_string(timeout_ms) + " ms");
+    return PCISPH_OK;
+}
+
 int pcisph_batch_scene_stats(pcisph_batch* b, int32_t id, pcisph_step_stats* out) {
     if (!b || !out) return report_error(PCISPH_ERR_INVALID_ARG, "NULL argument");
     const int k = b->find(id);

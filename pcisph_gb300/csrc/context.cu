@@ -1059,6 +1059,16 @@ int pcisph_sync(pcisph_ctx* ctx) {
     return PCISPH_OK;
 }
 
+int pcisph_sync_for(pcisph_ctx* ctx, int64_t timeout_ms) {
+    if (!ctx) return fail(PCISPH_ERR_INVALID_ARG, "ctx is NULL");
+    if (timeout_ms < 0) return fail(PCISPH_ERR_INVALID_ARG, "timeout_ms must be >= 0");
+    DeviceGuard g(ctx->device);
+    bool done = false;
+    CUDA_TRY(host::wait_stream_for(ctx->stream(), timeout_ms, &done));
+    if (!done) return fail(PCISPH_ERR_TIMEOUT, "queued steps still running after " + std::to_string(timeout_ms) + " ms");
+    return PCISPH_OK;
+}
+
 int pcisph_last_stats(pcisph_ctx* ctx, pcisph_step_stats* out) {
     if (!ctx || !out) return fail(PCISPH_ERR_INVALID_ARG, "NULL argument");
     DeviceGuard g(ctx->device);

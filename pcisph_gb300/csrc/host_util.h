@@ -3,9 +3,11 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdint>
 #include <string>
+#include <thread>
 
 #include "../../include/pcisph_gpu.h"
 #include "common.cuh"
@@ -21,6 +23,25 @@ inline size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 inline constexpr float kPi = 3.14159265358979323846f;  // utils/constants.h:4
 inline constexpr uint32_t kListCap = 96;           // neighbour-list entries per particle (multiple of 4)
 inline constexpr uint32_t kNearCap = 64;           // within-h list entries per particle
+
+// Wait up to timeout_ms for the work queued on s (0: look once). *done = false when it is still running at
+// the deadline; the work is left queued and a later wait can pick it up.
+inline cudaError_t wait_stream_for(cudaStream_t s, int64_t timeout_ms, bool* done) {
+    const auto deadline = std::chrono::steady_clock::now() + std::chrono::milliseconds(timeout_ms);
+    for (;;) {
+        const cudaError_t e = cudaStreamQuery(s);
+        if (e == cudaSuccess) {
+            *done = true;
+            return cudaSuccess;
+        }
+        if (e != cudaErrorNotReady) return e;
+        if (std::chrono::steady_clock::now() >= deadline) {
+            *done = false;
+            return cudaSuccess;
+        }
+        std::this_thread::sleep_for(std::chrono::microseconds(50));
+    }
+}
 
 // Fluid.cpp:125-133
 inline uint32_t sort_bit_count_ref(uint32_t elements) {

@@ -145,8 +145,13 @@ class Fluid:
     def step(self, n):
         check(self._L.pcisph_step(self._h, int(n)))
 
-    def sync(self):
-        check(self._L.pcisph_sync(self._h))
+    def sync(self, timeout_ms=None):
+        """Wait for the queued steps; with timeout_ms, raise PcisphError (code ERR_TIMEOUT) if they are
+        still running after that many milliseconds (the work stays queued)."""
+        if timeout_ms is None:
+            check(self._L.pcisph_sync(self._h))
+        else:
+            check(self._L.pcisph_sync_for(self._h, int(timeout_ms)))
 
     def stats(self):
         s = _lib.StepStats()

@@ -7,7 +7,9 @@ batch step with its own convergence loop, and a scene leaves the batch after its
 state read back to the host. The batch compacts once per step for all scenes that left.
 
 Reported per request: queueing delay (arrival to admission) and rollout latency (arrival to final state on
-the host); per batch step: its duration. No counterpart in the reference, which steps one scene in a
+the host); per batch step: its duration. With step_timeout_ms, a batch step still running after that bound
+is reported as stalled (a bounded wait on the stream, pcisph_batch_sync_for) before the server waits on;
+nothing on the device is interrupted. No counterpart in the reference, which steps one scene in a
 render loop (main.cpp:185-223).
 """
 import math
@@ -18,6 +20,7 @@ from dataclasses import dataclass, field
 import numpy as np
 
 from . import scenes as _scenes
+from ._lib import ERR_TIMEOUT, PcisphError
 
 
 class Request:
@@ -124,6 +127,7 @@ class ServeReport:
     running_at_end: int = 0
     particle_steps: int = 0
     peak_particles: int = 0
+    stalled_steps: list = field(default_factory=list)  # batch-step indices that outlived step_timeout_ms
 
     def summary(self):
         lat = np.array([c.latency for c in self.completions]) if self.completions else np.zeros(0)
@@ -141,7 +145,7 @@ class ServeReport:
             "step_ms_p50": pct(st, 50), "step_ms_p99": pct(st, 99),
             "rollout_s_p50": pct(lat, 50), "rollout_s_p99": pct(lat, 99),
             "queueing_s_p50": pct(que, 50), "queueing_s_p99": pct(que, 99),
-            "peak_particles": self.peak_particles,
+            "peak_particles": self.peak_particles, "stalled_steps": len(self.stalled_steps),
         }
 
 
@@ -151,16 +155,18 @@ class Server:
     batch: a pcisph_gb300.Batch (or an object with its methods: add_scene, remove_scene, step, sync, stats,
     get_field). budget_bytes bounds the device memory of the admitted scenes through the batch memory
     model (bytes per particle, bytes per scene); max_particles and max_scenes are the pool's own limits.
+    step_timeout_ms: report batch steps that run longer (None: no watch).
     """
 
     def __init__(self, batch, budget_bytes, bytes_per_particle, bytes_per_scene, max_particles, max_scenes,
-                 keep_state=True, clock=time.perf_counter):
+                 keep_state=True, clock=time.perf_counter, step_timeout_ms=None):
         self.batch = batch
         self.budget = int(budget_bytes)
         self.bpp, self.bps = int(bytes_per_particle), int(bytes_per_scene)
         self.max_particles, self.max_scenes = int(max_particles), int(max_scenes)
         self.keep_state = keep_state
         self.clock = clock
+        self.step_timeout_ms = step_timeout_ms
         self.queue = deque()     # (request, arrival time on the run's clock), arrival order
         self.running = []        # _Running, admission order
         self.used_bytes = 0
@@ -224,7 +230,7 @@ class Server:
         pending = sorted(requests, key=lambda r: r.arrival)
         pi = 0
         self._t0 = self.clock()
-        completions, step_ms, rejected = [], [], []
+        completions, step_ms, rejected, stalled = [], [], [], []
         admitted = particle_steps = peak = 0
         while True:
             now = self.clock_now()
@@ -248,7 +254,16 @@ class Server:
                 break
             t0 = self.clock()
             self.batch.step(1)
-            self.batch.sync()
+            if self.step_timeout_ms is None:
+                self.batch.sync()
+            else:
+                try:
+                    self.batch.sync(timeout_ms=self.step_timeout_ms)
+                except PcisphError as e:
+                    if e.code != ERR_TIMEOUT:
+                        raise
+                    stalled.append(len(step_ms))
+                    self.batch.sync()
             step_ms.append((self.clock() - t0) * 1e3)
             particle_steps += self.used_particles
             peak = max(peak, self.used_particles)
@@ -256,4 +271,4 @@ class Server:
                 r.left -= 1
             completions += self._retire(self.clock_now())
         return ServeReport(completions, step_ms, self.clock_now(), admitted, rejected, len(self.queue),
-                           len(self.running), particle_steps, peak)
+                           len(self.running), particle_steps, peak, stalled)

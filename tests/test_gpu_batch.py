@@ -163,3 +163,18 @@ def test_batch_autotune_leaves_results_unchanged():
         bt.close()
     for s, a, b in zip(sc, out[0], out[1]):
         _assert_same(s.name, b, a)
+
+
+def test_batch_bounded_sync():
+    from pcisph_gb300._lib import ERR_TIMEOUT
+    a = scenes.small_dam(40, seed=3)
+    bt = Batch(0, max_particles=2 * a.fluid_count, max_scenes=2)
+    ids = [bt.add_scene(a) for _ in range(2)]
+    bt.step(1)
+    bt.sync()
+    bt.step(100)
+    with pytest.raises(PcisphError) as e:
+        bt.sync(timeout_ms=0)
+    assert e.value.code == ERR_TIMEOUT
+    bt.sync(timeout_ms=600000)
+    assert all(bt.stats(i).steps == 101 for i in ids)

@@ -500,3 +500,24 @@ def test_autotune_leaves_the_simulation_unchanged():
     for n in out[0][0]:
         np.testing.assert_array_equal(out[1][0][n], out[0][0][n], err_msg=n)
     assert out[0][1] == out[1][1]
+
+
+def test_bounded_sync_reports_running_work():
+    """pcisph_sync_for: ERR_TIMEOUT while queued steps still run (nothing cancelled), OK once they end."""
+    from pcisph_gb300 import setup_scene
+    from pcisph_gb300._lib import ERR_INVALID_ARG, ERR_TIMEOUT, PcisphError
+    sc = scenes.small_dam(40, seed=3)  # 64,000 particles: ~0.5 ms a step, 200 steps queued in ~2 ms of host time
+    f = Fluid(0)
+    setup_scene(f, sc)
+    f.step(1)
+    f.sync()
+    f.step(200)
+    with pytest.raises(PcisphError) as e:
+        f.sync(timeout_ms=0)
+    assert e.value.code == ERR_TIMEOUT
+    f.sync(timeout_ms=600000)
+    assert f.stats().steps == 201
+    with pytest.raises(PcisphError) as e:
+        f.sync(timeout_ms=-1)
+    assert e.value.code == ERR_INVALID_ARG
+    f.close()

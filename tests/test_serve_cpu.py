@@ -41,7 +41,7 @@ class FakeBatch:
         for v in self.live.values():
             v[1] += n
 
-    def sync(self):
+    def sync(self, timeout_ms=None):
         pass
 
     def stats(self, sid):
@@ -142,3 +142,43 @@ def test_requests_shard_over_two_gloo_ranks(tmp_path):
     sizes = np.load(tmp_path / "sizes.npy")
     assert rids.tolist() == list(range(30))  # every request served once, by exactly one rank
     assert sizes.tolist() == [15, 15]
+
+
+def test_stalled_steps_are_reported_and_waited_out():
+    """step_timeout_ms: a batch step whose bounded wait times out is recorded as stalled, the server then
+    waits for it, and every request still completes with its own step count."""
+    from pcisph_gb300._lib import ERR_INVALID_ARG, ERR_TIMEOUT, PcisphError
+
+    class SlowBatch(FakeBatch):
+        def __init__(self, *a, slow=(), fail=None):
+            super().__init__(*a)
+            self.steps_done, self.slow, self.fail, self.waits = 0, set(slow), fail, []
+
+        def step(self, n=1):
+            super().step(n)
+            self.steps_done += n
+
+        def sync(self, timeout_ms=None):
+            self.waits.append(timeout_ms)
+            k = self.steps_done - 1
+            if timeout_ms is not None and k == self.fail:
+                raise PcisphError(ERR_INVALID_ARG, "not a timeout")
+            if timeout_ms is not None and k in self.slow:
+                raise PcisphError(ERR_TIMEOUT, "still running")
+
+    reqs = _tiny_requests(10)
+    bpp, bps = 10, 100
+    budget = 4 * 400 * bpp
+    fb = SlowBatch(budget, bpp, bps, slow=(1, 4))
+    srv = Server(fb, budget, bpp, bps, max_particles=10**6, max_scenes=64, step_timeout_ms=250)
+    rep = srv.run(reqs, realtime=False)
+    assert rep.stalled_steps == [1, 4] and rep.summary()["stalled_steps"] == 2
+    assert sorted(c.rid for c in rep.completions) == list(range(10))
+    for c in rep.completions:
+        assert c.steps == reqs[c.rid].steps and np.all(c.position == c.steps)
+    assert fb.waits.count(None) == 2 and fb.waits.count(250) == len(rep.step_ms)
+    # any other error of the bounded wait propagates
+    fb = SlowBatch(budget, bpp, bps, fail=2)
+    srv = Server(fb, budget, bpp, bps, max_particles=10**6, max_scenes=64, step_timeout_ms=250)
+    with pytest.raises(PcisphError):
+        srv.run(_tiny_requests(10), realtime=False)
