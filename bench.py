@@ -535,14 +535,14 @@ def main():
     kernels = {k: {"launches": l, "avg_us": 1e3 * ms / l, "share": ms / tot,
                    "algo_GBps": algo.get(k, 0) * N / (ms / l / 1e3) / 1e9} for k, (l, ms) in prof.items()}
 
-    # e2e through the C ABI with pinned host buffers, over the same first steps
+    # e2e through the C ABI with pinned host buffers, over the same steps as the timed loop
     pos_h = torch.empty((N, 3), dtype=torch.float32, pin_memory=True).numpy()
     vel_h = torch.empty((N, 3), dtype=torch.float32, pin_memory=True).numpy()
     f.set_fluid_state(snap_pos, snap_vel)
     f.get_field("position", out=pos_h)
     f.get_field("velocity", out=vel_h)
     start_pos, start_vel = pos_h.copy(), vel_h.copy()
-    e2e_steps = prof_steps
+    e2e_steps = args.steps
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
