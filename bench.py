@@ -574,6 +574,9 @@ def main():
                        "kernel_variant": args.variant, "loop_mode": args.loop_mode, "autotuned": tuned,
                        "mean_iterations": iters, "particle_iterations_per_s": value * iters,
                        "max_density_error_last": st1.max_density_error,
+                       "list_skin": f.get_options().list_skin,
+                       "list_fallback_sweeps_per_step": (st1.list_fallbacks - st0.list_fallbacks) / args.steps,
+                       "fast_predictions_per_step": (st1.fast_particles - st0.fast_particles) / args.steps,
                        "step_ms_min_median_max": [min(step_ms), statistics.median(step_ms), max(step_ms)],
                        "converged_all_steps": (status_bits & 1) == 0, "status_bits": status_bits,
                        "l2": "256 MB written between timed steps (not timed); step working set ~200 MB > L2",
