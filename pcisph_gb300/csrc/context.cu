@@ -148,6 +148,7 @@ struct pcisph_ctx {
         order_n = n;
         order_bk = bk;
         graph_valid = false;
+        order_age = kNoOrder;
         return PCISPH_OK;
     }
 
@@ -155,17 +156,22 @@ struct pcisph_ctx {
     // the particles gathered into it. Returns the launches issued, or -1.
     int record_working_order(const uint32_t* sk, const uint32_t* sv, cudaStream_t s) {
         const uint32_t N = params.fluid_count, BK = params.bucket_count;
-        if (cudaMemsetAsync(bucket_codes, 0xFF, (size_t)BK * 4, s) != cudaSuccess) return -1;
+        const bool reuse = reuse_order_now && bucket_order;
+        if (!reuse && cudaMemsetAsync(bucket_codes, 0xFF, (size_t)BK * 4, s) != cudaSuccess) return -1;
         int nl = 0;
         timed("reorder", s, [&] { launch_bucket_codes(sk, sv, b.state_pos, N, P, b.cells, bucket_codes, b.ctl, s); });
         ++nl;
-        uint32_t *ok = nullptr, *order = nullptr;
-        cudaError_t e = cudaSuccess;
-        timed("bucket_sort", s, [&] {
-            e = bucket_sorter.sort(bucket_codes, bucket_ids, BK, 24, true, s, &ok, &order);
-            nl += bucket_sorter.last_launches();
-        });
-        if (e != cudaSuccess) return -1;
+        if (!reuse) {
+            uint32_t *ok = nullptr, *order = nullptr;
+            cudaError_t e = cudaSuccess;
+            timed("bucket_sort", s, [&] {
+                e = bucket_sorter.sort(bucket_codes, bucket_ids, BK, 24, true, s, &ok, &order);
+                nl += bucket_sorter.last_launches();
+            });
+            if (e != cudaSuccess) return -1;
+            bucket_order = order;
+        }
+        const uint32_t* order = bucket_order;
         timed("working_ranges", s, [&] { launch_working_ranges(order, BK, b.cells, cells_w, range_scratch, N, s); });
         timed("permute", s, [&] {
             launch_permute(sk, sv, b.state_pos, b.state_vel, N, BK, b.cells, cells_w, b.pos, b.vel, d_of_w, w_of_d,
@@ -207,12 +213,24 @@ struct pcisph_ctx {
         b.bucket_fast = c.take<unsigned char>(params.bucket_count);
         list_n = n;
         graph_valid = false;
+        order_age = kNoOrder;
         return PCISPH_OK;
     }
 
 
-    cudaGraphExec_t graph_exec = nullptr;
+    cudaGraphExec_t graph_exec = nullptr;        // the step, bucket sort included
+    cudaGraphExec_t graph_exec_reuse = nullptr;  // the step reusing the last bucket order (working order on)
     bool graph_valid = false;
+    // The working order's bucket placement (the bucket sort's output) is refreshed every kOrderRefresh steps
+    // and reused in between: any placement of whole buckets keeps every sum, only locality ages as
+    // particles change cells. order_age: steps since the last bucket sort ran, kNoOrder when none ran for
+    // the current buffers and graphs.
+    static constexpr uint32_t kOrderRefresh = 8;
+    static constexpr uint32_t kNoOrder = 0xFFFFFFFFu;
+    uint32_t order_age = kNoOrder;
+    bool reuse_order_now = false;   // record_working_order: keep bucket_order instead of sorting
+    const uint32_t* bucket_order = nullptr;  // bucket ids in Morton order of their cells (the last bucket sort)
+    int prefix_launches_reuse = 0;
     uint64_t host_launches = 0;
     uint64_t host_mode_iters = 0;  // corrective iterations run by the host-driven loop
     cudaStream_t own_stream = nullptr;
@@ -263,6 +281,7 @@ struct pcisph_ctx {
         sorted_keys = f_keys;
         sorted_ids = f_ids;
         graph_valid = false;
+        order_age = kNoOrder;
         return ensure_shared(std::max(n, boundary_cap_n));
     }
 
@@ -285,6 +304,7 @@ struct pcisph_ctx {
         boundary_cap_n = n;
         boundary_cap_bk = bk;
         graph_valid = false;
+        order_age = kNoOrder;
         return ensure_shared(std::max(n, fluid_cap_n));
     }
 
@@ -295,6 +315,7 @@ struct pcisph_ctx {
                 return fail(PCISPH_ERR_OOM, "device allocation of the sort scratch failed");
             sorter.set_scratch(sort_block.p, sort_block.cap);
             graph_valid = false;
+            order_age = kNoOrder;
         }
         if (staging_block.ensure((size_t)std::max<uint32_t>(n, 1) * 16) != cudaSuccess)
             return fail(PCISPH_ERR_OOM, "device allocation of the staging buffer failed");
@@ -306,6 +327,7 @@ struct pcisph_ctx {
         make_devparams(params, opts.min_iterations, opts.max_iterations, opts.walls, opts.box_lo, opts.box_hi,
                        opts.restitution, threshold, opts.list_skin, 0, &P);
         graph_valid = false;
+        order_age = kNoOrder;
     }
 
     // update_deduced_attributes: derive, (re)allocate, zero velocities, mark the boundary for sorting.
@@ -461,10 +483,26 @@ struct pcisph_ctx {
     }
 
     int build_graph() {
-        if (graph_exec) {
-            cudaGraphExecDestroy(graph_exec);
-            graph_exec = nullptr;
+        for (cudaGraphExec_t* g : {&graph_exec, &graph_exec_reuse})
+            if (*g) {
+                cudaGraphExecDestroy(*g);
+                *g = nullptr;
+            }
+        reuse_order_now = false;
+        int rc = capture_graph(&graph_exec, &prefix_launches);
+        if (rc) return rc;
+        if (working_order()) {  // the same step without the bucket sort
+            reuse_order_now = true;
+            rc = capture_graph(&graph_exec_reuse, &prefix_launches_reuse);
+            reuse_order_now = false;
+            if (rc) return rc;
         }
+        order_age = kNoOrder;  // the first launch sorts the buckets
+        graph_valid = true;
+        return PCISPH_OK;
+    }
+
+    int capture_graph(cudaGraphExec_t* exec, int* prefix_nl) {
         const bool prof = profiling;
         profiling = false;
         cudaStream_t s = capture_stream;
@@ -480,12 +518,11 @@ struct pcisph_ctx {
                 return fail(PCISPH_ERR_CUDA, std::string("graph capture of the persistent step failed: ") +
                                                  cudaGetErrorString(le != cudaSuccess ? le : ee));
             }
-            prefix_launches = nl + 1;
+            *prefix_nl = nl + 1;
             iter_launches = 0;
-            cudaError_t ie = cudaGraphInstantiate(&graph_exec, graph, 0);
+            cudaError_t ie = cudaGraphInstantiate(exec, graph, 0);
             cudaGraphDestroy(graph);
             if (ie != cudaSuccess) return fail(PCISPH_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ie));
-            graph_valid = true;
             return PCISPH_OK;
         }
         cudaStreamCaptureStatus st;
@@ -500,7 +537,7 @@ struct pcisph_ctx {
             return fail(PCISPH_ERR_CUDA, std::string("graph capture of the step failed: ") +
                                              cudaGetErrorString(e != cudaSuccess ? e : e2));
         }
-        prefix_launches = nl;
+        *prefix_nl = nl;
         cudaGraphConditionalHandle handle;
         CUDA_TRY(cudaGraphConditionalHandleCreate(&handle, graph, 1, cudaGraphCondAssignDefault));
         cudaGraphNodeParams cp{};
@@ -517,10 +554,9 @@ struct pcisph_ctx {
         profiling = prof;
         cudaGraph_t body_out = nullptr;
         CUDA_TRY(cudaStreamEndCapture(s, &body_out));
-        e = cudaGraphInstantiate(&graph_exec, graph, 0);
+        e = cudaGraphInstantiate(exec, graph, 0);
         cudaGraphDestroy(graph);
         if (e != cudaSuccess) return fail(PCISPH_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
-        graph_valid = true;
         return PCISPH_OK;
     }
 
@@ -560,13 +596,19 @@ struct pcisph_ctx {
                 rc = build_graph();
                 if (rc) return rc;
             }
-            CUDA_TRY(cudaGraphLaunch(graph_exec, s));
-            host_launches += prefix_launches;
+            const bool full = !graph_exec_reuse || order_age >= kOrderRefresh;
+            CUDA_TRY(cudaGraphLaunch(full ? graph_exec : graph_exec_reuse, s));
+            host_launches += full ? prefix_launches : prefix_launches_reuse;
+            order_age = full ? 1u : order_age + 1u;
             ++steps_launched;
             return PCISPH_OK;
         }
-        // host-driven loop (Fluid.cpp:250-307)
+        // host-driven loop (Fluid.cpp:250-307), on the same bucket-order schedule as the graphs
+        const bool full = !working_order() || order_age >= kOrderRefresh;
+        reuse_order_now = !full;
         int nl = record_prefix(s);
+        reuse_order_now = false;
+        order_age = full ? 1u : order_age + 1u;
         if (nl < 0) return fail(PCISPH_ERR_CUDA, std::string("step launch failed: ") + cudaGetErrorString(cudaGetLastError()));
         host_launches += nl;
         ++steps_launched;
@@ -815,6 +857,7 @@ struct pcisph_ctx {
         DeviceGuard g(device);
         if (user_stream) cudaStreamSynchronize(user_stream);
         if (graph_exec) cudaGraphExecDestroy(graph_exec);
+        if (graph_exec_reuse) cudaGraphExecDestroy(graph_exec_reuse);
         for (auto& p : pending) {
             cudaEventDestroy(p.a);
             cudaEventDestroy(p.b);
@@ -944,6 +987,7 @@ int pcisph_set_density_variation_threshold(pcisph_ctx* ctx, float t) {  // Fluid
     ctx->threshold = t;
     ctx->P.threshold = t;
     ctx->graph_valid = false;
+    ctx->order_age = pcisph_ctx::kNoOrder;
     return PCISPH_OK;
 }
 
@@ -1266,6 +1310,7 @@ int pcisph_autotune(pcisph_ctx* ctx, uint32_t steps, pcisph_tune_result* out) {
         ctx->sorted_keys = ctx->f_keys;  // no view into the released scratch survives
         ctx->sorted_ids = ctx->f_ids;
         ctx->graph_valid = false;
+        ctx->order_age = pcisph_ctx::kNoOrder;
         return ctx->ensure_shared(std::max(N, ctx->boundary_cap_n));
     };
     auto time_it = [&](float* ms) -> int {

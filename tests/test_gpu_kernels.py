@@ -415,7 +415,7 @@ def test_working_order_changes_no_result(case):
     for so in (0, 1):
         f = Fluid(0)
         setup_scene(f, sc, kernel_variant=2, spatial_order=so)
-        f.step(8)
+        f.step(20)  # bucket order refreshed at steps 1, 9, 17 and reused in between
         st = f.stats()
         out.append(({n: f.get_field(n) for n in names}, (st.total_iterations, st.status_all, st.fast_particles)))
         f.close()
