@@ -548,8 +548,7 @@ def main():
     for _ in range(e2e_steps):
         f.set_fluid_state(pos_h, vel_h)
         f.update()
-        f.get_field("position", out=pos_h)
-        f.get_field("velocity", out=vel_h)
+        f.get_fluid_state(pos_h, vel_h)
     e2e_s = time.perf_counter() - t0
     e2e = {"value": N * e2e_steps * world / e2e_s, "unit": "particle-steps/s", "h2d_bytes_per_step": 24 * N,
            "d2h_bytes_per_step": 24 * N, "steps": e2e_steps,

@@ -218,6 +218,11 @@ PCISPH_API int pcisph_reset_stats(pcisph_ctx* ctx);
 
 /* Export. dst_bytes must cover count x layout; HOST copies synchronise. */
 PCISPH_API int pcisph_get_field(pcisph_ctx* ctx, int field, void* dst, size_t dst_bytes, int layout, int memory);
+/* The counterpart of pcisph_set_fluid_state: positions and velocities (either may be NULL) in one call with
+ * one synchronisation. Pinned host buffers (cudaHostAlloc / cudaHostRegister) are written by the layout
+ * conversion kernel directly, as pinned sources are read by pcisph_set_fluid_state; other host memory goes
+ * through a device staging buffer. */
+PCISPH_API int pcisph_get_fluid_state(pcisph_ctx* ctx, float* pos, float* vel, uint32_t count, int layout, int memory);
 /* Overwrite one field (parity tests feed identical inputs to a stage). */
 PCISPH_API int pcisph_set_field(pcisph_ctx* ctx, int field, const void* src, size_t src_bytes, int layout, int memory);
 /* Zero-copy view (replaces the CL-GL shared buffers): device pointer, element count, native layout. */

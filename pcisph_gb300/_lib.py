@@ -145,6 +145,7 @@ def load():
         "pcisph_last_stats": ([vp, C.POINTER(StepStats)], i32),
         "pcisph_reset_stats": ([vp], i32),
         "pcisph_get_field": ([vp, i32, vp, sz, i32, i32], i32),
+        "pcisph_get_fluid_state": ([vp, vp, vp, u32, i32, i32], i32),
         "pcisph_set_field": ([vp, i32, vp, sz, i32, i32], i32),
         "pcisph_field_device_ptr": ([vp, i32, C.POINTER(vp), C.POINTER(sz), C.POINTER(i32)], i32),
         "pcisph_run_stage": ([vp, i32, i32], i32),

@@ -758,8 +758,12 @@ struct pcisph_ctx {
         } else if (layout == PCISPH_LAYOUT_PACKED3) {
             const float* dsrc = src;
             if (memory == PCISPH_MEM_HOST) {
-                CUDA_TRY(cudaMemcpyAsync(staging_block.p, src, n * 12, cudaMemcpyHostToDevice, s));
-                dsrc = static_cast<const float*>(staging_block.p);
+                if (const void* dv = host::pinned_device_view(src)) {
+                    dsrc = static_cast<const float*>(dv);  // the conversion reads the pinned buffer itself
+                } else {
+                    CUDA_TRY(cudaMemcpyAsync(staging_block.p, src, n * 12, cudaMemcpyHostToDevice, s));
+                    dsrc = static_cast<const float*>(staging_block.p);
+                }
             }
             launch_pack3_to4(dsrc, dst, (uint32_t)n, s);
             ++host_launches;
@@ -770,7 +774,8 @@ struct pcisph_ctx {
         return PCISPH_OK;
     }
 
-    int get_field(int field, void* dst, size_t dst_bytes, int layout, int memory) {
+    // sync = false: a HOST copy is left queued (the caller synchronises)
+    int get_field(int field, void* dst, size_t dst_bytes, int layout, int memory, bool sync = true) {
         FieldView v;
         if (!field_view(field, &v)) return fail(PCISPH_ERR_INVALID_ARG, "unknown field " + std::to_string(field));
         if (!v.ptr) return fail(PCISPH_ERR_NOT_READY, "field not allocated yet (set the state or call update first)");
@@ -794,15 +799,17 @@ struct pcisph_ctx {
             v.ptr = xfer;
         }
         if (layout == PCISPH_LAYOUT_PACKED3) {
-            float* out = memory == PCISPH_MEM_HOST ? static_cast<float*>(staging_block.p) : static_cast<float*>(dst);
+            void* pinned = memory == PCISPH_MEM_HOST ? host::pinned_device_view(dst) : nullptr;
+            float* out = memory == PCISPH_MEM_HOST ? static_cast<float*>(pinned ? pinned : staging_block.p)
+                                                   : static_cast<float*>(dst);
             launch_unpack4_to3(static_cast<const float4*>(v.ptr), out, (uint32_t)v.count, s);
             ++host_launches;
             CUDA_TRY(cudaGetLastError());
-            if (memory == PCISPH_MEM_HOST) CUDA_TRY(cudaMemcpyAsync(dst, out, need, kind, s));
+            if (memory == PCISPH_MEM_HOST && !pinned) CUDA_TRY(cudaMemcpyAsync(dst, out, need, kind, s));
         } else {
             CUDA_TRY(cudaMemcpyAsync(dst, v.ptr, need, kind, s));
         }
-        if (memory == PCISPH_MEM_HOST) CUDA_TRY(cudaStreamSynchronize(s));
+        if (memory == PCISPH_MEM_HOST && sync) CUDA_TRY(cudaStreamSynchronize(s));
         return PCISPH_OK;
     }
 
@@ -1025,6 +1032,25 @@ int pcisph_prepare(pcisph_ctx* ctx) {
     if (!ctx) return fail(PCISPH_ERR_INVALID_ARG, "ctx is NULL");
     DeviceGuard g(ctx->device);
     return ctx->params_changed ? ctx->derive_now() : PCISPH_OK;
+}
+
+int pcisph_get_fluid_state(pcisph_ctx* ctx, float* pos, float* vel, uint32_t count, int layout, int memory) {
+    if (!ctx) return fail(PCISPH_ERR_INVALID_ARG, "ctx is NULL");
+    if (count && !pos && !vel) return fail(PCISPH_ERR_INVALID_ARG, "pos and vel are NULL");
+    if (layout != PCISPH_LAYOUT_PACKED3 && layout != PCISPH_LAYOUT_FLOAT4)
+        return fail(PCISPH_ERR_INVALID_ARG, "positions take PACKED3 or FLOAT4");
+    if (memory != PCISPH_MEM_HOST && memory != PCISPH_MEM_DEVICE) return fail(PCISPH_ERR_INVALID_ARG, "bad memory kind");
+    if (count != ctx->params.fluid_count)
+        return fail(PCISPH_ERR_INCONSISTENT, "Inconsistent positions_size (" + std::to_string(count) + ") for " +
+                                                 std::to_string(ctx->params.fluid_count) + " particles");
+    DeviceGuard g(ctx->device);
+    const size_t bytes = (size_t)count * (layout == PCISPH_LAYOUT_PACKED3 ? 12 : 16);
+    int rc = PCISPH_OK;
+    if (pos) rc = ctx->get_field(PCISPH_FIELD_POSITION, pos, bytes, layout, memory, false);
+    if (!rc && vel) rc = ctx->get_field(PCISPH_FIELD_VELOCITY, vel, bytes, layout, memory, false);
+    if (rc) return rc;
+    if (memory == PCISPH_MEM_HOST) CUDA_TRY(cudaStreamSynchronize(ctx->stream()));
+    return PCISPH_OK;
 }
 
 int pcisph_set_fluid_state(pcisph_ctx* ctx, const float* pos, const float* vel, uint32_t count, int layout,

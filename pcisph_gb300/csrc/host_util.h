@@ -43,6 +43,18 @@ inline cudaError_t wait_stream_for(cudaStream_t s, int64_t timeout_ms, bool* don
     }
 }
 
+// The device address of pinned host memory (cudaHostAlloc / cudaHostRegister: mapped into the device's
+// address space), or null for pageable or device memory. Kernels may read and write pinned buffers
+// through it directly (over the host link), without a staging copy.
+inline void* pinned_device_view(const void* p) {
+    cudaPointerAttributes a{};
+    if (!p || cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
 // Fluid.cpp:125-133
 inline uint32_t sort_bit_count_ref(uint32_t elements) {
     uint32_t max_value = 0;

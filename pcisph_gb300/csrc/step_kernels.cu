@@ -347,21 +347,47 @@ __global__ void __launch_bounds__(kBlock) k_pack_boundary(DevParams P, const flo
     bpf[i] = make_float4(x.x, x.y, x.z, b_press[i] / (P.rest_density * P.rest_density));
 }
 
+// Packed float3 <-> float4. A block moves its 256 elements' 768 packed floats as three fully coalesced
+// rows (thread t: floats t, t + 256, t + 512) through shared memory (stride-3 element access there is
+// conflict-free), so every request covers whole 128-byte lines: this matters most when the packed side is
+// pinned host memory read or written over the host link.
 __global__ void __launch_bounds__(kBlock) k_pack3_to4(const float* __restrict__ in3, float4* __restrict__ out,
                                                       uint32_t n) {
-    const uint32_t i = blockIdx.x * kBlock + threadIdx.x;
-    if (i >= n) return;
-    out[i] = make_float4(in3[3 * (size_t)i], in3[3 * (size_t)i + 1], in3[3 * (size_t)i + 2], 0.f);
+    __shared__ float tile[3 * kBlock];
+    const size_t base = (size_t)blockIdx.x * kBlock;
+    const size_t total = 3 * (size_t)n;
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+        const size_t k = 3 * base + r * kBlock + threadIdx.x;
+        if (k < total) tile[r * kBlock + threadIdx.x] = in3[k];
+    }
+    __syncthreads();
+    const size_t i = base + threadIdx.x;
+    if (i < n) {
+        const float* e = &tile[3 * threadIdx.x];
+        out[i] = make_float4(e[0], e[1], e[2], 0.f);
+    }
 }
 
 __global__ void __launch_bounds__(kBlock) k_unpack4_to3(const float4* __restrict__ in, float* __restrict__ out3,
                                                         uint32_t n) {
-    const uint32_t i = blockIdx.x * kBlock + threadIdx.x;
-    if (i >= n) return;
-    const float4 v = in[i];
-    out3[3 * (size_t)i] = v.x;
-    out3[3 * (size_t)i + 1] = v.y;
-    out3[3 * (size_t)i + 2] = v.z;
+    __shared__ float tile[3 * kBlock];
+    const size_t base = (size_t)blockIdx.x * kBlock;
+    const size_t i = base + threadIdx.x;
+    if (i < n) {
+        const float4 v = in[i];
+        float* e = &tile[3 * threadIdx.x];
+        e[0] = v.x;
+        e[1] = v.y;
+        e[2] = v.z;
+    }
+    __syncthreads();
+    const size_t total = 3 * (size_t)n;
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+        const size_t k = 3 * base + r * kBlock + threadIdx.x;
+        if (k < total) out3[k] = tile[r * kBlock + threadIdx.x];
+    }
 }
 
 }  // namespace

@@ -237,6 +237,25 @@ class Fluid:
         check(self._L.pcisph_get_field(self._h, FIELDS[name], _ptr(arr), arr.nbytes, lay, _lib.MEM_HOST))
         return arr
 
+    def get_fluid_state(self, pos=None, vel=None, layout="packed3"):
+        """Positions and velocities in one call (one synchronisation), into ``pos`` / ``vel`` (numpy or
+        device tensors of n x 3 or n x 4 floats) or new numpy arrays. Returns (pos, vel)."""
+        n = self._count("position")
+        lay = _lib.LAYOUT_PACKED3 if layout == "packed3" else _lib.LAYOUT_FLOAT4
+        if pos is None:
+            pos = np.empty((n, 3 if lay == _lib.LAYOUT_PACKED3 else 4), np.float32)
+        if vel is None:
+            vel = np.empty_like(pos)
+        dev = _is_device(pos)
+        if dev != _is_device(vel):
+            raise ValueError("pos and vel must both be host arrays or both device tensors")
+        for a in (pos, vel):
+            if (a.numel() * a.element_size() if dev else a.nbytes) < n * (12 if lay == _lib.LAYOUT_PACKED3 else 16):
+                raise ValueError("output too small")
+        check(self._L.pcisph_get_fluid_state(self._h, _ptr(pos), _ptr(vel), n, lay,
+                                             _lib.MEM_DEVICE if dev else _lib.MEM_HOST))
+        return pos, vel
+
     def set_field(self, name, arr):
         if _is_device(arr):
             mem, nbytes = _lib.MEM_DEVICE, arr.numel() * arr.element_size()
