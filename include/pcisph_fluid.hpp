@@ -67,6 +67,11 @@ class Fluid {
         check(pcisph_set_boundary_state(ctx_, pos.data(), static_cast<uint32_t>(pos.size() / 3),
                                         PCISPH_LAYOUT_PACKED3, PCISPH_MEM_HOST));
     }
+    // Positions and velocities back into caller buffers of count x 3 floats, one synchronisation (pinned
+    // buffers are written directly by the device).
+    void get_fluid_state(float* pos, float* vel, uint32_t count) {
+        check(pcisph_get_fluid_state(ctx_, pos, vel, count, PCISPH_LAYOUT_PACKED3, PCISPH_MEM_HOST));
+    }
     // A field copied to the host: vectors packed xyz, scalars one value per particle.
     std::vector<float> field(pcisph_field f) {
         void* p = nullptr;
