@@ -46,6 +46,7 @@ ALGO_BYTES = {
 # 60, cell reset 4, reorder 60, density 20, normal 32, force 72, integrate 72; per iteration predict 60,
 # pressure 40, pressure force 36), vectors at their 12-byte payload
 STEP_FIXED_BYTES = 340
+CPU_POINTS = 8  # states of the timed run the CPU baseline samples from
 STEP_ITER_BYTES = 136
 DAM_WORKLOADS = {
     "dam1m": ("config1", "particle-steps/s @1M (<=1% rho err)",
@@ -219,6 +220,32 @@ def cpu_step_rate(scene, pos, vel, seconds, max_steps=None):
         steps += 1
         iters.append(st.iterations)
     return scene.fluid_count * steps / t_total, steps, float(np.mean(iters)), s
+
+
+def cpu_sample_rate(scene, states, seconds):
+    """Oracle steps from each of `states` ((pos, vel) at several points of a run) in rounds, one step per
+    state per round, until `seconds` of step time; returns (particle-steps/s, steps, mean iterations)."""
+    import numpy as np
+
+    from oracle.oracle import get as get_oracle
+    from oracle.oracle import make_options
+    O = get_oracle()
+    p = O.derive_params(scene.particle_radius, scene.rest_density, scene.fluid_count, 0, scene.delta_t,
+                        scene.gravity, scene.viscosity_constant(), scene.surface_tension)
+    opts = make_options(threshold=scene.threshold, min_iters=scene.min_iters, max_iters=scene.max_iters,
+                        walls=scene.walls, box_lo=scene.box_lo, box_hi=scene.box_hi, restitution=scene.restitution)
+    runs = [O.new_state(p, pos, vel) for pos, vel in states]
+    t_total, steps, iters = 0.0, 0, []
+    while t_total < seconds:
+        for s in runs:
+            t0 = time.perf_counter()
+            st = O.step(p, opts, s)
+            t_total += time.perf_counter() - t0
+            steps += 1
+            iters.append(st.iterations)
+            if t_total >= seconds:
+                break
+    return scene.fluid_count * steps / t_total, steps, float(np.mean(iters))
 
 
 def reference_arm(args, rank, world):
@@ -541,15 +568,23 @@ def main():
     f.set_fluid_state(snap_pos, snap_vel)
     f.get_field("position", out=pos_h)
     f.get_field("velocity", out=vel_h)
-    start_pos, start_vel = pos_h.copy(), vel_h.copy()
     e2e_steps = args.steps
+    # the CPU baseline starts from the states at evenly spaced points of these steps (the copies are not
+    # timed), so that it samples the same part of the run as the GPU's timed steps
+    points = sorted({(k * e2e_steps) // CPU_POINTS for k in range(CPU_POINTS)})
+    samples = []
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    for _ in range(e2e_steps):
+    t_copy = 0.0
+    for k in range(e2e_steps):
+        if k in points:
+            tc = time.perf_counter()
+            samples.append((pos_h.copy(), vel_h.copy()))
+            t_copy += time.perf_counter() - tc
         f.set_fluid_state(pos_h, vel_h)
         f.update()
         f.get_fluid_state(pos_h, vel_h)
-    e2e_s = time.perf_counter() - t0
+    e2e_s = time.perf_counter() - t0 - t_copy
     e2e = {"value": N * e2e_steps * world / e2e_s, "unit": "particle-steps/s", "h2d_bytes_per_step": 24 * N,
            "d2h_bytes_per_step": 24 * N, "steps": e2e_steps,
            "device_value_same_steps": N * e2e_steps * world / (sum(step_ms[:e2e_steps]) / 1e3)}
@@ -558,10 +593,11 @@ def main():
     step_bytes = STEP_FIXED_BYTES + STEP_ITER_BYTES * iters
     cpu = None
     if rank == 0 and world == 1:
-        rate, csteps, citers, _ = cpu_step_rate(sc, start_pos, start_vel, args.cpu_seconds, max_steps=args.steps)
+        rate, csteps, citers = cpu_sample_rate(sc, samples, args.cpu_seconds)
         cpu = {"value": rate, "unit": "particle-steps/s", "cores": os.cpu_count(), "kind": "port",
-               "sample": f"{N} particles x the first {csteps} of the timed steps, from the same state "
-                         f"(mean {citers:.2f} corrective iterations), oracle/pcisph_oracle.cpp with OpenMP",
+               "sample": f"{N} particles x {csteps} steps, one step at a time from the states at {len(samples)} "
+                         f"evenly spaced points of the timed steps (mean {citers:.2f} corrective iterations "
+                         f"against the GPU's {iters:.2f}), oracle/pcisph_oracle.cpp with OpenMP",
                "mean_iterations": citers, "particle_iterations_per_s": rate * citers}
     if rank == 0:
         line = {

@@ -80,3 +80,17 @@ def test_walk_candidates_counts_the_27_bucket_walk():
             b = key(c[0] + k % 3 - 1, c[1] + (k // 3) % 3 - 1, c[2] + k // 9 - 1)
             want += int(off[b, 1]) - int(off[b, 0])
     assert bench.walk_candidates(F()) == pytest.approx(want / n, rel=1e-12)
+
+
+def test_cpu_sample_rate_steps_every_state():
+    """bench.cpu_sample_rate: rounds of one oracle step per sampled state until the time bound."""
+    import bench
+    from pcisph_gb300 import scenes
+    sc = scenes.small_dam(6, seed=2)
+    pos = sc.fluid_pos.astype(np.float32)
+    vel = np.zeros_like(pos)
+    states = [(pos, vel), (pos + np.float32(0.001), vel)]
+    rate, steps, iters = bench.cpu_sample_rate(sc, states, seconds=1e-9)
+    assert steps == 1 and rate > 0 and sc.min_iters <= iters <= sc.max_iters
+    rate, steps, iters = bench.cpu_sample_rate(sc, states, seconds=0.05)
+    assert steps >= 1 and rate > 0
