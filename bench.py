@@ -84,6 +84,8 @@ def parse():
                     help="run the library's autotuner on the warmed-up state before timing (results unchanged)")
     ap.add_argument("--loop-mode", type=int, default=0, choices=[0, 2],
                     help="corrective loop: 0 graph WHILE node, 2 persistent cooperative kernel")
+    ap.add_argument("--spatial-order", type=int, default=2, choices=[0, 1, 2],
+                    help="pcisph_options.spatial_order of the dam-break workloads (2: the library's choice)")
     return ap.parse_args()
 
 
@@ -498,7 +500,7 @@ def main():
     stream = torch.cuda.Stream()  # a real stream: the library launches on it, the events are recorded on it
     torch.cuda.set_stream(stream)
     f = Fluid(local, stream=stream.cuda_stream)
-    setup_scene(f, sc, kernel_variant=args.variant, loop_mode=args.loop_mode)
+    setup_scene(f, sc, kernel_variant=args.variant, loop_mode=args.loop_mode, spatial_order=args.spatial_order)
     sampler = ClockSampler(local)
     sampler.start()
     for _ in range(args.warmup):
