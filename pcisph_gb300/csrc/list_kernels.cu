@@ -265,8 +265,10 @@ __device__ __forceinline__ float pressure_body(const PS& ps, const ListBuffers& 
         const float4 xp = b.pred[i];
         float acc = 0.f;
         const uint32_t cnt = b.nbr_count[i];
-        const Cell c = cell_of(xi.x, xi.y, xi.z, P);
-        const bool walk = cnt > P.list_cap || (!all_lists_ok && near_fast(P, b.bucket_fast, c));
+        const bool overflow = cnt > P.list_cap;
+        Cell c{0u, 0u, 0u};  // the cell (three IEEE divisions) only where a walk may need it
+        if (overflow || !all_lists_ok || P.boundary_count) c = cell_of(xi.x, xi.y, xi.z, P);
+        const bool walk = overflow || (!all_lists_ok && near_fast(P, b.bucket_fast, c));
         if (P.boundary_count)
             for_each_neighbour(b.b_cells, c, P, [&](uint32_t j) { acc += density_term(xp.x, xp.y, xp.z, __ldg(&b.b_pos[j]), P.h2); });
         auto f = [&](uint32_t j) { acc += density_term(xp.x, xp.y, xp.z, __ldg(&b.pred[j]), P.h2); };
