@@ -224,9 +224,10 @@ def cpu_step_rate(scene, pos, vel, seconds, max_steps=None):
     return scene.fluid_count * steps / t_total, steps, float(np.mean(iters)), s
 
 
-def cpu_sample_rate(scene, states, seconds):
-    """Oracle steps from each of `states` ((pos, vel) at several points of a run) in rounds, one step per
-    state per round, until `seconds` of step time; returns (particle-steps/s, steps, mean iterations)."""
+def cpu_sample_rate(scene, states, seconds, max_steps=None):
+    """Oracle steps from each of `states` ((pos, vel) at evenly spaced points of a run) in rounds, one step
+    per state per round, until `seconds` of step time or `max_steps` steps (the run's length: each state
+    then covers its own segment of the run); returns (particle-steps/s, steps, mean iterations)."""
     import numpy as np
 
     from oracle.oracle import get as get_oracle
@@ -238,14 +239,14 @@ def cpu_sample_rate(scene, states, seconds):
                         walls=scene.walls, box_lo=scene.box_lo, box_hi=scene.box_hi, restitution=scene.restitution)
     runs = [O.new_state(p, pos, vel) for pos, vel in states]
     t_total, steps, iters = 0.0, 0, []
-    while t_total < seconds:
+    while t_total < seconds and (max_steps is None or steps < max_steps):
         for s in runs:
             t0 = time.perf_counter()
             st = O.step(p, opts, s)
             t_total += time.perf_counter() - t0
             steps += 1
             iters.append(st.iterations)
-            if t_total >= seconds:
+            if t_total >= seconds or (max_steps is not None and steps >= max_steps):
                 break
     return scene.fluid_count * steps / t_total, steps, float(np.mean(iters))
 
@@ -595,7 +596,7 @@ def main():
     step_bytes = STEP_FIXED_BYTES + STEP_ITER_BYTES * iters
     cpu = None
     if rank == 0 and world == 1:
-        rate, csteps, citers = cpu_sample_rate(sc, samples, args.cpu_seconds)
+        rate, csteps, citers = cpu_sample_rate(sc, samples, args.cpu_seconds, max_steps=args.steps)
         cpu = {"value": rate, "unit": "particle-steps/s", "cores": os.cpu_count(), "kind": "port",
                "sample": f"{N} particles x {csteps} steps, one step at a time from the states at {len(samples)} "
                          f"evenly spaced points of the timed steps (mean {citers:.2f} corrective iterations "
