@@ -208,15 +208,17 @@ def test_full_steps_vs_reference(golden, case, loop_mode, variant):
         k += 1
 
 
-@pytest.mark.parametrize("variant", [0, 2])
-def test_graph_and_host_loop_identical(variant):
+@pytest.mark.parametrize("variant,order", [(0, 0), (2, 0), (2, 1)])
+def test_graph_and_host_loop_identical(variant, order):
+    """Loop modes (graph WHILE node, host loop, persistent kernel) give the same bits; with the working
+    order on, 12 steps run through one bucket-placement refresh and the reuse in between."""
     sc = scenes.small_dam(10, seed=3)
     out = []
     for mode in ((0, 1, 2) if variant == 2 else (0, 1)):
         f = Fluid(0)
         from pcisph_gb300 import setup_scene
-        setup_scene(f, sc, loop_mode=mode, kernel_variant=variant)
-        f.step(5)
+        setup_scene(f, sc, loop_mode=mode, kernel_variant=variant, spatial_order=order)
+        f.step(12 if order else 5)
         st = f.stats()
         out.append((f.get_field("position"), f.get_field("velocity"), f.get_field("pressure"), st.total_iterations))
     for other in out[1:]:
@@ -559,3 +561,30 @@ def test_pinned_host_buffers_take_the_direct_path():
     for a, b in zip(out[0], out[1]):
         np.testing.assert_array_equal(a, b)
     f.close()
+
+
+def test_reused_bucket_placement_after_a_new_state():
+    """A state set in the middle of a run is stepped with the previous steps' bucket placement (refreshed
+    only every 8 steps): the sums are those of a fresh context, bit for bit, also in the profiled host loop."""
+    from pcisph_gb300 import setup_scene
+    a = scenes.small_dam(12, seed=7)
+    b = scenes.small_dam(12, seed=8)
+    b.fluid_pos = (b.fluid_pos + np.float32(0.05)).astype(np.float32)  # a different arrangement, same count
+    names = ("position", "velocity", "density", "pressure")
+    f = Fluid(0)
+    setup_scene(f, a, spatial_order=1)
+    f.step(3)
+    f.set_fluid_state(b.fluid_pos, np.zeros_like(b.fluid_pos))
+    f.step(4)
+    f.profile(True)
+    f.step(3)
+    f.profile(False)
+    got = {n: f.get_field(n) for n in names}
+    g = Fluid(0)
+    setup_scene(g, b, spatial_order=1)
+    g.step(7)
+    want = {n: g.get_field(n) for n in names}
+    for n in names:
+        np.testing.assert_array_equal(got[n], want[n], err_msg=n)
+    f.close()
+    g.close()
