@@ -98,6 +98,8 @@ typedef struct pcisph_options {
                                       buckets in Morton order of their cells (every sum unchanged; state and
                                       exported fields stay in the reference's sorted order); 0: sorted order;
                                       2 (default): 1 from 131,072 particles, else 0 */
+    int32_t sweep_block;           /* variant 2: threads per block of the pressure and pressure-force sweeps
+                                      (the corrective loop's kernels): 128, 256 (default) or 512 */
 } pcisph_options;
 
 typedef struct pcisph_step_stats {
@@ -241,6 +243,7 @@ typedef struct pcisph_tune_result {
     float list_skin;
     int32_t spatial_order;
     int32_t digit_bits;
+    int32_t sweep_block;
     float ms_per_step;          /* the chosen candidate */
     float ms_per_step_before;   /* the settings on entry */
     int32_t candidates;

@@ -50,7 +50,7 @@ class Options(C.Structure):
     _fields_ = [("min_iterations", C.c_int32), ("max_iterations", C.c_int32), ("walls", C.c_int32),
                 ("box_lo", C.c_float * 3), ("box_hi", C.c_float * 3), ("restitution", C.c_float),
                 ("boundary_self_density", C.c_int32), ("loop_mode", C.c_int32), ("kernel_variant", C.c_int32),
-                ("list_skin", C.c_float), ("spatial_order", C.c_int32)]
+                ("list_skin", C.c_float), ("spatial_order", C.c_int32), ("sweep_block", C.c_int32)]
 
 
 class StepStats(C.Structure):
@@ -75,6 +75,7 @@ class Camera(C.Structure):
 
 class TuneResult(C.Structure):
     _fields_ = [("list_skin", C.c_float), ("spatial_order", C.c_int32), ("digit_bits", C.c_int32),
+                ("sweep_block", C.c_int32),
                 ("ms_per_step", C.c_float), ("ms_per_step_before", C.c_float), ("candidates", C.c_int32)]
 
 

@@ -468,8 +468,10 @@ struct pcisph_ctx {
             ++nl;
         }
         if (list_sweeps()) {
-            timed("pressure", s, [&] { launch_pressure_list(P, b.ctl, list_buffers(), s); });
-            timed("pressure_force", s, [&] { launch_pressure_force_list(P, b.ctl, list_buffers(), 0, cond, use_cond, s); });
+            timed("pressure", s, [&] { launch_pressure_list(P, b.ctl, list_buffers(), opts.sweep_block, s); });
+            timed("pressure_force", s, [&] {
+                launch_pressure_force_list(P, b.ctl, list_buffers(), 0, cond, use_cond, opts.sweep_block, s);
+            });
         } else if (warp_sweeps()) {
             const SweepArgs A = sweep_args();
             timed("pressure", s, [&] { launch_pressure_sweep(P, b, A, sweep_grid, s); });
@@ -691,13 +693,14 @@ struct pcisph_ctx {
                 break;
             case PCISPH_STAGE_BOUNDARY_PRESSURE: launch_boundary_pressure(P, b, working_order() ? cells_w : b.cells, s); ++host_launches; break;
             case PCISPH_STAGE_PRESSURE:
-                if (list_sweeps()) launch_pressure_list(P, b.ctl, list_buffers(), s);
+                if (list_sweeps()) launch_pressure_list(P, b.ctl, list_buffers(), opts.sweep_block, s);
                 else if (warp_sweeps()) launch_pressure_sweep(P, b, sweep_args(), sweep_grid, s);
                 else launch_pressure(P, b, s);
                 ++host_launches;
                 break;
             case PCISPH_STAGE_PRESSURE_FORCE:
-                if (list_sweeps()) launch_pressure_force_list(P, b.ctl, list_buffers(), arg ? 2 : 1, 0, false, s);
+                if (list_sweeps())
+                    launch_pressure_force_list(P, b.ctl, list_buffers(), arg ? 2 : 1, 0, false, opts.sweep_block, s);
                 else if (warp_sweeps()) launch_pressure_force_sweep(P, b, sweep_args(), sweep_grid, arg ? 2 : 1, 0, false, s);
                 else launch_pressure_force(P, b, arg ? 2 : 1, 0, false, s);
                 ++host_launches;
@@ -928,6 +931,7 @@ int pcisph_default_options(pcisph_options* o) {
     o->kernel_variant = 2;
     o->list_skin = 0.25f;
     o->spatial_order = 2;
+    o->sweep_block = 256;
     return PCISPH_OK;
 }
 
@@ -1009,6 +1013,8 @@ int pcisph_set_options(pcisph_ctx* ctx, const pcisph_options* o) {
         return fail(PCISPH_ERR_INVALID_ARG, "kernel_variant must be 0, 1 or 2");
     if (!(o->list_skin >= 0.f && o->list_skin <= 2.f))
         return fail(PCISPH_ERR_INVALID_ARG, "list_skin must be in [0, 2]");
+    if (o->sweep_block != 128 && o->sweep_block != 256 && o->sweep_block != 512)
+        return fail(PCISPH_ERR_INVALID_ARG, "sweep_block must be 128, 256 or 512");
     const bool bsd_changed = o->boundary_self_density != ctx->opts.boundary_self_density;
     ctx->opts = *o;
     if (bsd_changed) ctx->boundary_updated = true;
@@ -1325,10 +1331,11 @@ int pcisph_autotune(pcisph_ctx* ctx, uint32_t steps, pcisph_tune_result* out) {
         CUDA_TRY(cudaStreamSynchronize(s));
         return PCISPH_OK;
     };
-    auto apply = [&](float skin, int order, int bits) -> int {
+    auto apply = [&](float skin, int order, int bits, int block) -> int {
         pcisph_options o = ctx->opts;
         o.list_skin = skin;
         o.spatial_order = order;
+        o.sweep_block = block;
         int r = pcisph_set_options(ctx, &o);
         if (r) return r;
         ctx->sorter.set_digit_bits(bits);
@@ -1354,7 +1361,7 @@ int pcisph_autotune(pcisph_ctx* ctx, uint32_t steps, pcisph_tune_result* out) {
         return PCISPH_OK;
     };
     float before = 0.f;
-    rc = apply(entry.list_skin, entry_order, entry_bits);
+    rc = apply(entry.list_skin, entry_order, entry_bits, entry.sweep_block);
     if (!rc) rc = time_it(&before);
     float best_ms = before, best_skin = entry.list_skin;
     int best_order = entry_order, best_bits = entry_bits, n = 1;
@@ -1367,7 +1374,7 @@ int pcisph_autotune(pcisph_ctx* ctx, uint32_t steps, pcisph_tune_result* out) {
                 if (rc) break;
                 if (sk == entry.list_skin && od == entry_order && bt == entry_bits) continue;
                 float ms = 0.f;
-                rc = apply(sk, od, bt);
+                rc = apply(sk, od, bt, entry.sweep_block);
                 if (!rc) rc = time_it(&ms);
                 ++n;
                 if (!rc && ms < best_ms) {
@@ -1377,7 +1384,20 @@ int pcisph_autotune(pcisph_ctx* ctx, uint32_t steps, pcisph_tune_result* out) {
                     best_bits = bt;
                 }
             }
-    if (!rc) rc = apply(best_skin, best_order, best_bits);
+    // then the block size of the corrective-loop sweeps, on the best of the above
+    int best_block = entry.sweep_block;
+    for (int bl : {128, 256, 512}) {
+        if (rc || bl == entry.sweep_block) continue;
+        float ms = 0.f;
+        rc = apply(best_skin, best_order, best_bits, bl);
+        if (!rc) rc = time_it(&ms);
+        ++n;
+        if (!rc && ms < best_ms) {
+            best_ms = ms;
+            best_block = bl;
+        }
+    }
+    if (!rc) rc = apply(best_skin, best_order, best_bits, best_block);
     const int rc2 = restore();
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
@@ -1390,6 +1410,7 @@ int pcisph_autotune(pcisph_ctx* ctx, uint32_t steps, pcisph_tune_result* out) {
     out->list_skin = best_skin;
     out->spatial_order = best_order;
     out->digit_bits = best_bits;
+    out->sweep_block = best_block;
     out->ms_per_step = best_ms;
     out->ms_per_step_before = before;
     out->candidates = n;

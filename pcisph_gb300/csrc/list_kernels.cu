@@ -291,13 +291,14 @@ __device__ __forceinline__ float pressure_body(const PS& ps, const ListBuffers& 
     return dv;
 }
 
-template <class PS>
-__global__ void __launch_bounds__(kBlock) k_pressure_list(PS ps, ListBuffers b) {
-    const float dv = pressure_body(ps, b, blockIdx.x * kBlock + threadIdx.x);
+// BS: threads per block (128, 256 or 512; the autotuner's choice for one scene)
+template <class PS, int BS = kBlock>
+__global__ void __launch_bounds__(BS) k_pressure_list(PS ps, ListBuffers b) {
+    const float dv = pressure_body(ps, b, blockIdx.x * BS + threadIdx.x);
     if (PS::kBatched) return;
     // one scene: block max of dv, the last block decides (dv >= 0: bit patterns order like values)
     const unsigned bits = __reduce_max_sync(0xffffffffu, __float_as_uint(dv));
-    __shared__ unsigned warp_max[kBlock / 32];
+    __shared__ unsigned warp_max[BS / 32];
     __shared__ bool is_last;
     if ((threadIdx.x & 31) == 0) warp_max[threadIdx.x >> 5] = bits;
     __syncthreads();
@@ -305,7 +306,7 @@ __global__ void __launch_bounds__(kBlock) k_pressure_list(PS ps, ListBuffers b) 
     if (threadIdx.x == 0) {
         unsigned m = 0;
 #pragma unroll
-        for (int w = 0; w < kBlock / 32; ++w) m = max(m, warp_max[w]);
+        for (int w = 0; w < BS / 32; ++w) m = max(m, warp_max[w]);
         atomicMax(&ctl->max_err_bits, m);
         __threadfence();
         is_last = atomicAdd(&ctl->blocks_done, 1u) == gridDim.x - 1;
@@ -370,10 +371,10 @@ __device__ __forceinline__ void pressure_force_body(const PS& ps, const ListBuff
     b.state_vel[o] = f4(v, 0.f);
 }
 
-template <class PS>
-__global__ void __launch_bounds__(kBlock) k_pressure_force_list(PS ps, ListBuffers b, int mode,
-                                                                cudaGraphConditionalHandle cond, int use_cond) {
-    const uint32_t i = blockIdx.x * kBlock + threadIdx.x;
+template <class PS, int BS = kBlock>
+__global__ void __launch_bounds__(BS) k_pressure_force_list(PS ps, ListBuffers b, int mode,
+                                                            cudaGraphConditionalHandle cond, int use_cond) {
+    const uint32_t i = blockIdx.x * BS + threadIdx.x;
     if (!PS::kBatched && use_cond && i == 0) {
         // continue the graph's while loop unless the step is done; the counter bounds it on its own
         Control* ctl = ps.control(0);
@@ -525,13 +526,21 @@ void launch_normal_list(const DevParams& P, Control* ctl, const ListBuffers& b, 
 void launch_force_list(const DevParams& P, Control* ctl, const ListBuffers& b, cudaStream_t s) {
     k_force_list<<<grid_for(P.fluid_count), kBlock, 0, s>>>(OneScene{P, ctl}, b);
 }
-void launch_pressure_list(const DevParams& P, Control* ctl, const ListBuffers& b, cudaStream_t s) {
-    k_pressure_list<<<grid_for(P.fluid_count), kBlock, 0, s>>>(OneScene{P, ctl}, b);
+void launch_pressure_list(const DevParams& P, Control* ctl, const ListBuffers& b, int block, cudaStream_t s) {
+    const OneScene ps{P, ctl};
+    const uint32_t n = P.fluid_count;
+    if (block == 128) k_pressure_list<OneScene, 128><<<(n + 127) / 128, 128, 0, s>>>(ps, b);
+    else if (block == 512) k_pressure_list<OneScene, 512><<<(n + 511) / 512, 512, 0, s>>>(ps, b);
+    else k_pressure_list<OneScene, kBlock><<<grid_for(n), kBlock, 0, s>>>(ps, b);
 }
 void launch_pressure_force_list(const DevParams& P, Control* ctl, const ListBuffers& b, int mode,
-                                cudaGraphConditionalHandle cond, bool use_cond, cudaStream_t s) {
-    k_pressure_force_list<<<grid_for(P.fluid_count), kBlock, 0, s>>>(OneScene{P, ctl}, b, mode, cond,
-                                                                      use_cond ? 1 : 0);
+                                cudaGraphConditionalHandle cond, bool use_cond, int block, cudaStream_t s) {
+    const OneScene ps{P, ctl};
+    const uint32_t n = P.fluid_count;
+    const int uc = use_cond ? 1 : 0;
+    if (block == 128) k_pressure_force_list<OneScene, 128><<<(n + 127) / 128, 128, 0, s>>>(ps, b, mode, cond, uc);
+    else if (block == 512) k_pressure_force_list<OneScene, 512><<<(n + 511) / 512, 512, 0, s>>>(ps, b, mode, cond, uc);
+    else k_pressure_force_list<OneScene, kBlock><<<grid_for(n), kBlock, 0, s>>>(ps, b, mode, cond, uc);
 }
 
 namespace {

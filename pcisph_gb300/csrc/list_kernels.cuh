@@ -59,10 +59,11 @@ struct SceneTable {
 void launch_density_list(const DevParams& P, Control* ctl, const ListBuffers& b, cudaStream_t s);
 void launch_normal_list(const DevParams& P, Control* ctl, const ListBuffers& b, cudaStream_t s);
 void launch_force_list(const DevParams& P, Control* ctl, const ListBuffers& b, cudaStream_t s);
-void launch_pressure_list(const DevParams& P, Control* ctl, const ListBuffers& b, cudaStream_t s);
+// block: threads per block of the two corrective-loop sweeps (128, 256 or 512)
+void launch_pressure_list(const DevParams& P, Control* ctl, const ListBuffers& b, int block, cudaStream_t s);
 // mode 0: the loop decision picks predict or integrate; 1: predict; 2: integrate
 void launch_pressure_force_list(const DevParams& P, Control* ctl, const ListBuffers& b, int mode,
-                                cudaGraphConditionalHandle cond, bool use_cond, cudaStream_t s);
+                                cudaGraphConditionalHandle cond, bool use_cond, int block, cudaStream_t s);
 
 void launch_batch_begin(Control* ctls, uint32_t n_scenes, Control* batch, cudaStream_t s);
 void launch_scene_of(const uint32_t* offsets, uint32_t n_scenes, uint32_t n, uint16_t* scene_of, cudaStream_t s);

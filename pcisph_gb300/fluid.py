@@ -162,11 +162,13 @@ class Fluid:
         check(self._L.pcisph_reset_stats(self._h))
 
     def autotune(self, steps=3):
-        """Pick the fastest list skin / working order / sort digit width on the current state (results are
-        unchanged by any choice); returns the choice and the step times."""
+        """Pick the fastest list skin / working order / sort digit width, then the corrective-loop sweeps'
+        block size, on the current state (results are unchanged by any choice); returns the choice and the
+        step times."""
         r = _lib.TuneResult()
         check(self._L.pcisph_autotune(self._h, int(steps), C.byref(r)))
         return {"list_skin": r.list_skin, "spatial_order": r.spatial_order, "digit_bits": r.digit_bits,
+                "sweep_block": r.sweep_block,
                 "ms_per_step": r.ms_per_step, "ms_per_step_before": r.ms_per_step_before,
                 "candidates": r.candidates}
 

@@ -492,8 +492,9 @@ def test_autotune_leaves_the_simulation_unchanged():
         f.step(3)
         if tune:
             r = f.autotune(steps=2)
-            assert r["candidates"] == 16 and r["ms_per_step"] <= r["ms_per_step_before"]
+            assert r["candidates"] == 18 and r["ms_per_step"] <= r["ms_per_step_before"]
             assert f.get_options().list_skin == pytest.approx(r["list_skin"])
+            assert f.get_options().sweep_block == r["sweep_block"] in (128, 256, 512)
         f.step(5)
         st = f.stats()
         out.append(({n: f.get_field(n) for n in ("position", "velocity", "density")},
@@ -588,3 +589,23 @@ def test_reused_bucket_placement_after_a_new_state():
         np.testing.assert_array_equal(got[n], want[n], err_msg=n)
     f.close()
     g.close()
+
+
+@pytest.mark.parametrize("block", [128, 512])
+def test_sweep_block_size_changes_no_result(block):
+    """The corrective-loop sweeps at 128 or 512 threads per block compute the bits of the default 256."""
+    from pcisph_gb300 import setup_scene
+    sc = scenes.small_dam(14, seed=5)
+    out = []
+    for bl in (256, block):
+        f = Fluid(0)
+        setup_scene(f, sc, spatial_order=1)
+        f.set_options(sweep_block=bl)
+        f.step(6)
+        st = f.stats()
+        out.append(({n: f.get_field(n) for n in ("position", "velocity", "density", "pressure")},
+                    (st.total_iterations, st.status_all)))
+        f.close()
+    for n in out[0][0]:
+        np.testing.assert_array_equal(out[1][0][n], out[0][0][n], err_msg=n)
+    assert out[0][1] == out[1][1]
