@@ -334,6 +334,31 @@ def scenes_workload(args, rank, world, local):
     iters = [(b.total_iterations - a.total_iterations) / args.steps for a, b in zip(st0, st1)]
     batch_loop_iters = max(iters)
 
+    # per-kernel CUDA events over the first timed steps again (profiled host-driven steps, same kernels)
+    for i, (p, v) in zip(ids, snap):
+        bt.set_state(i, p, v)
+    prof_steps = min(args.steps, 20)
+    sp0 = [bt.stats(i) for i in ids]
+    bt.profile(True)
+    bt.step(prof_steps)
+    prof = bt.profile_read()
+    bt.profile(False)
+    sp1 = [bt.stats(i) for i in ids]
+    # particle-iterations of the profiled steps: the pressure sweeps' work
+    p_iters = sum(s.fluid_count * (b.total_iterations - a.total_iterations) for s, a, b in zip(sc, sp0, sp1))
+    tot_ms = sum(ms for _, ms in prof.values())
+    kernels = {k: {"launches": l, "avg_us": 1e3 * ms / l, "share": ms / tot_ms} for k, (l, ms) in prof.items()}
+    roof = None
+    if "pressure" in prof:
+        peak, peak_kind = peaks()
+        l, ms = prof["pressure"]
+        achieved = ALGO_BYTES["pressure"] * p_iters / (ms / 1e3) / 1e9
+        roof = {"bound": "hbm", "kernel": "pressure", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None,
+                "algo_bytes_per_particle": ALGO_BYTES["pressure"], "avg_launch_us": 1e3 * ms / l,
+                "note": "algorithmic bytes of the particle-iterations of the profiled steps over the total time "
+                        "of their pressure sweeps (finished scenes skip)"}
+
     # e2e through the batch ABI: host state of every scene in, one step, every scene's state out
     e2e_steps = min(args.steps, 5)
     pin = [(torch.empty((s.fluid_count, 3), dtype=torch.float32, pin_memory=True).numpy(),
@@ -401,7 +426,7 @@ def scenes_workload(args, rank, world, local):
                                    "speedup_of_batch": ms_single / ms_batch},
             "e2e": {"value": n_total * e2e_steps * world / e2e_s, "unit": "particle-steps/s",
                     "h2d_bytes_per_step": 24 * n_total, "d2h_bytes_per_step": 24 * n_total, "steps": e2e_steps},
-            "gpu_launches": launches, "cpu_baseline": cpu, "clocks": clocks,
+            "gpu_launches": launches, "roofline": roof, "kernels": kernels, "cpu_baseline": cpu, "clocks": clocks,
         }
         print(json.dumps(line), flush=True)
 

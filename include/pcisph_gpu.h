@@ -329,6 +329,10 @@ PCISPH_API int pcisph_batch_info(const pcisph_batch* batch, uint32_t* scenes, ui
 /* steps time steps of every scene (one CUDA graph launch each; no host synchronisation). */
 PCISPH_API int pcisph_batch_step(pcisph_batch* batch, uint32_t steps);
 PCISPH_API int pcisph_batch_sync(pcisph_batch* batch);
+/* Per-kernel timing of a batch, as pcisph_profile_enable / _read: while enabled, steps run host-driven (the
+ * same kernels as the step graph, the loop's continuation read back each iteration), every launch timed. */
+PCISPH_API int pcisph_batch_profile_enable(pcisph_batch* batch, int enable);
+PCISPH_API int pcisph_batch_profile_read(pcisph_batch* batch, pcisph_kernel_time* out, int max_entries, int* n_entries);
 /* pcisph_sync_for for a batch's stream. */
 PCISPH_API int pcisph_batch_sync_for(pcisph_batch* batch, int64_t timeout_ms);
 /* Synchronises, then reports the scene's last step (and totals since it was added). */

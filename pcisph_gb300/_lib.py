@@ -174,6 +174,8 @@ def load():
         "pcisph_batch_info": ([vp, C.POINTER(u32), C.POINTER(u32), C.POINTER(u32)], i32),
         "pcisph_batch_step": ([vp, u32], i32),
         "pcisph_batch_sync": ([vp], i32),
+        "pcisph_batch_profile_enable": ([vp, i32], i32),
+        "pcisph_batch_profile_read": ([vp, C.POINTER(KernelTime), i32, C.POINTER(i32)], i32),
         "pcisph_batch_sync_for": ([vp, C.c_int64], i32),
         "pcisph_batch_scene_stats": ([vp, C.c_int32, C.POINTER(StepStats)], i32),
         "pcisph_batch_get_field": ([vp, C.c_int32, i32, vp, sz, i32, i32], i32),

@@ -107,6 +107,18 @@ class Batch:
     def step(self, n=1):
         check(self._L.pcisph_batch_step(self._h, int(n)))
 
+    def profile(self, enable=True):
+        """While enabled, steps run host-driven with every launch timed (same kernels, same results)."""
+        check(self._L.pcisph_batch_profile_enable(self._h, int(bool(enable))))
+
+    def profile_read(self):
+        """{kernel name: (launches, total ms)} of the profiled steps."""
+        n = C.c_int()
+        check(self._L.pcisph_batch_profile_read(self._h, None, 0, C.byref(n)))
+        arr = (_lib.KernelTime * max(1, n.value))()
+        check(self._L.pcisph_batch_profile_read(self._h, arr, n.value, C.byref(n)))
+        return {arr[i].name.decode(): (int(arr[i].launches), float(arr[i].total_ms)) for i in range(n.value)}
+
     def sync(self, timeout_ms=None):
         """Wait for the queued steps; with timeout_ms, raise PcisphError (ERR_TIMEOUT) if they are still
         running after that many milliseconds (the work stays queued)."""

@@ -77,12 +77,21 @@ struct pcisph_batch {
     uint64_t host_launches = 0;
     int prefix_launches = 0, iter_launches = 3;
     uint32_t *sorted_keys = nullptr, *sorted_ids = nullptr;
+    bool profiling = false;   // steps run host-driven, every launch timed
+    host::KernelTimer timer;
 
     cudaStream_t stream() const { return user_stream; }
+
+    template <class F>
+    void timed(const char* name, cudaStream_t s, F&& f) {
+        if (profiling) timer.timed(name, s, f);
+        else f();
+    }
 
     ~pcisph_batch() {
         DeviceGuard g(device);
         if (user_stream) cudaStreamSynchronize(user_stream);
+        timer.release();
         if (graph_exec) cudaGraphExecDestroy(graph_exec);
         pool.release();
         tables.release();
@@ -243,20 +252,24 @@ struct pcisph_batch {
         ++nl;
         if (cudaMemsetAsync(cells, 0, (size_t)n_buckets * 8, s) != cudaSuccess) return -1;
         if (cudaMemsetAsync(bucket_fast, 0, n_buckets, s) != cudaSuccess) return -1;
-        launch_hash_scenes(t, state_pos, keys, s);
+        timed("hash", s, [&] { launch_hash_scenes(t, state_pos, keys, s); });
         ++nl;
         uint32_t *sk = nullptr, *sv = nullptr;
-        if (sorter.sort(keys, ids, n_particles, key_bits(n_buckets), true, s, &sk, &sv) != cudaSuccess) return -1;
+        cudaError_t se = cudaSuccess;
+        timed("radix_sort", s, [&] { se = sorter.sort(keys, ids, n_particles, key_bits(n_buckets), true, s, &sk, &sv); });
+        if (se != cudaSuccess) return -1;
         nl += sorter.last_launches();
         sorted_keys = sk;
         sorted_ids = sv;
         DevParams R{};
         R.bucket_count = n_buckets;
-        launch_reorder(sk, sv, state_pos, state_vel, n_particles, pos, vel, cells, nullptr, nullptr, R, d_batch, s);
+        timed("reorder", s, [&] {
+            launch_reorder(sk, sv, state_pos, state_vel, n_particles, pos, vel, cells, nullptr, nullptr, R, d_batch, s);
+        });
         const ListBuffers b = list_buffers();
-        launch_density_scenes(t, b, s);
-        launch_normal_scenes(t, b, s);
-        launch_force_scenes(t, b, s);
+        timed("density", s, [&] { launch_density_scenes(t, b, s); });
+        timed("normal", s, [&] { launch_normal_scenes(t, b, s); });
+        timed("force", s, [&] { launch_force_scenes(t, b, s); });
         nl += 4;
         return cudaGetLastError() == cudaSuccess ? nl : -1;
     }
@@ -364,10 +377,48 @@ struct pcisph_batch {
             int rc = build_graph();
             if (rc) return rc;
         }
+        if (profiling) {
+            for (uint32_t k = 0; k < steps; ++k) {
+                int rc = step_profiled();
+                if (rc) return rc;
+            }
+            return PCISPH_OK;
+        }
         for (uint32_t k = 0; k < steps; ++k) {
             BTRY(cudaGraphLaunch(graph_exec, stream()));
             host_launches += prefix_launches;
         }
+        return PCISPH_OK;
+    }
+
+    // One step launched from the host with every launch timed: the same kernels as the graph, and the
+    // loop's continuation read back after each iteration (as the graph's WHILE node reads it on the device).
+    int step_profiled() {
+        cudaStream_t s = stream();
+        const int nl = record_prefix(s);
+        if (nl < 0) return report_error(PCISPH_ERR_CUDA, std::string("batch step: ") + cudaGetErrorString(cudaGetLastError()));
+        host_launches += nl;
+        const SceneTable t = scene_table();
+        const ListBuffers b = list_buffers();
+        iter_launches = loop_mode == 2 ? 0 : 3;  // counted on the device per iteration (total_iters)
+        if (loop_mode == 2) {
+            cudaError_t le = cudaSuccess;
+            timed("corrective_loop", s, [&] { le = launch_corrective_loop_scenes(t, b, d_batch, max_iters, s); });
+            if (le != cudaSuccess) return report_error(PCISPH_ERR_CUDA, std::string("persistent loop: ") + cudaGetErrorString(le));
+            ++host_launches;
+        } else {
+            for (int it = 0; it < max_iters; ++it) {
+                timed("pressure", s, [&] { launch_pressure_scenes(t, b, s); });
+                timed("decide", s, [&] { launch_batch_decide(t, d_batch, max_iters, 0, false, s); });
+                timed("pressure_force", s, [&] { launch_pressure_force_scenes(t, b, s); });
+                unsigned running = 0;
+                BTRY(cudaMemcpyAsync(&running, &d_batch->any_running, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+                BTRY(cudaStreamSynchronize(s));
+                if (!running) break;
+            }
+        }
+        BTRY(cudaGetLastError());
+        timer.collect(s);
         return PCISPH_OK;
     }
 
@@ -717,6 +768,22 @@ int pcisph_batch_graph_stats(const pcisph_batch* b, uint64_t* instantiations, ui
     if (!b) return report_error(PCISPH_ERR_INVALID_ARG, "batch is NULL");
     if (instantiations) *instantiations = b->graph_instantiations;
     if (updates) *updates = b->graph_updates;
+    return PCISPH_OK;
+}
+
+int pcisph_batch_profile_enable(pcisph_batch* b, int enable) {
+    if (!b) return report_error(PCISPH_ERR_INVALID_ARG, "batch is NULL");
+    b->profiling = enable != 0;
+    if (enable) b->timer.clear();
+    return PCISPH_OK;
+}
+
+int pcisph_batch_profile_read(pcisph_batch* b, pcisph_kernel_time* out, int max_entries, int* n_entries) {
+    if (!b) return report_error(PCISPH_ERR_INVALID_ARG, "batch is NULL");
+    DeviceGuard g(b->device);
+    b->timer.collect(b->stream());
+    const int n = b->timer.read(out, max_entries);
+    if (n_entries) *n_entries = n;
     return PCISPH_OK;
 }
 

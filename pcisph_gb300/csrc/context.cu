@@ -58,11 +58,6 @@ size_t boundary_arena_bytes(uint32_t n, uint32_t bk) {
     return 3 * align256((size_t)n * 16) + 5 * align256((size_t)n * 4) + align256((size_t)bk * 8);
 }
 
-struct KernelTiming {
-    uint64_t launches = 0;
-    double ms = 0.0;
-};
-
 }  // namespace
 
 struct pcisph_ctx {
@@ -239,13 +234,7 @@ struct pcisph_ctx {
     int iter_launches = 0;
 
     bool profiling = false;
-    std::map<std::string, KernelTiming> timings;
-    struct Pending {
-        std::string name;
-        cudaEvent_t a, b;
-    };
-    std::vector<Pending> pending;
-    std::vector<cudaEvent_t> event_pool;
+    host::KernelTimer timer;  // per-kernel times of the profiled (host-driven) steps
 
     cudaStream_t stream() const { return user_stream; }
 
@@ -345,42 +334,12 @@ struct pcisph_ctx {
     }
 
     // -------------------------------------------------------------- timing
-    cudaEvent_t take_event() {
-        if (!event_pool.empty()) {
-            cudaEvent_t e = event_pool.back();
-            event_pool.pop_back();
-            return e;
-        }
-        cudaEvent_t e;
-        cudaEventCreate(&e);
-        return e;
-    }
     template <class F>
     void timed(const char* name, cudaStream_t s, F&& f) {
-        if (!profiling) {
-            f();
-            return;
-        }
-        Pending p{name, take_event(), take_event()};
-        cudaEventRecord(p.a, s);
-        f();
-        cudaEventRecord(p.b, s);
-        pending.push_back(p);
+        if (profiling) timer.timed(name, s, f);
+        else f();
     }
-    void collect_timings() {
-        if (pending.empty()) return;
-        cudaStreamSynchronize(stream());
-        for (auto& p : pending) {
-            float ms = 0.f;
-            cudaEventElapsedTime(&ms, p.a, p.b);
-            auto& t = timings[p.name];
-            t.launches += 1;
-            t.ms += ms;
-            event_pool.push_back(p.a);
-            event_pool.push_back(p.b);
-        }
-        pending.clear();
-    }
+    void collect_timings() { timer.collect(stream()); }
 
     // ---------------------------------------------------------------- sort
     int sort_set(const float4* pos_in, uint32_t n, uint32_t* keys, uint32_t* ids, uint32_t** sk, uint32_t** sv,
@@ -868,11 +827,7 @@ struct pcisph_ctx {
         if (user_stream) cudaStreamSynchronize(user_stream);
         if (graph_exec) cudaGraphExecDestroy(graph_exec);
         if (graph_exec_reuse) cudaGraphExecDestroy(graph_exec_reuse);
-        for (auto& p : pending) {
-            cudaEventDestroy(p.a);
-            cudaEventDestroy(p.b);
-        }
-        for (auto e : event_pool) cudaEventDestroy(e);
+        timer.release();
         fluid_block.release();
         boundary_block.release();
         misc_block.release();
@@ -1467,7 +1422,7 @@ uint64_t pcisph_kernel_launches(const pcisph_ctx* ctx) {
 int pcisph_profile_enable(pcisph_ctx* ctx, int enable) {
     if (!ctx) return fail(PCISPH_ERR_INVALID_ARG, "ctx is NULL");
     ctx->profiling = enable != 0;
-    if (enable) ctx->timings.clear();
+    if (enable) ctx->timer.clear();
     return PCISPH_OK;
 }
 
@@ -1475,16 +1430,7 @@ int pcisph_profile_read(pcisph_ctx* ctx, pcisph_kernel_time* out, int max_entrie
     if (!ctx) return fail(PCISPH_ERR_INVALID_ARG, "ctx is NULL");
     DeviceGuard g(ctx->device);
     ctx->collect_timings();
-    int n = 0;
-    for (auto& kv : ctx->timings) {
-        if (out && n < max_entries) {
-            std::memset(out[n].name, 0, sizeof(out[n].name));
-            std::strncpy(out[n].name, kv.first.c_str(), sizeof(out[n].name) - 1);
-            out[n].launches = kv.second.launches;
-            out[n].total_ms = kv.second.ms;
-        }
-        ++n;
-    }
+    const int n = ctx->timer.read(out, max_entries);
     if (n_entries) *n_entries = n;
     return PCISPH_OK;
 }

@@ -6,8 +6,11 @@
 #include <chrono>
 #include <cmath>
 #include <cstdint>
+#include <cstring>
+#include <map>
 #include <string>
 #include <thread>
+#include <vector>
 
 #include "../../include/pcisph_gpu.h"
 #include "common.cuh"
@@ -54,6 +57,84 @@ inline void* pinned_device_view(const void* p) {
     }
     return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
 }
+
+// Per-kernel CUDA-event timing of host-launched work (the profiled step paths): timed() brackets a launch
+// with two pooled events on its stream; collect() waits for the stream and adds the elapsed times up per
+// name.
+class KernelTimer {
+   public:
+    struct Total {
+        uint64_t launches = 0;
+        double ms = 0.0;
+    };
+    template <class F>
+    void timed(const char* name, cudaStream_t s, F&& f) {
+        Pending p{name, take(), take()};
+        cudaEventRecord(p.a, s);
+        f();
+        cudaEventRecord(p.b, s);
+        pending_.push_back(p);
+    }
+    void collect(cudaStream_t s) {
+        if (pending_.empty()) return;
+        cudaStreamSynchronize(s);
+        for (auto& p : pending_) {
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, p.a, p.b);
+            Total& t = totals_[p.name];
+            t.launches += 1;
+            t.ms += ms;
+            pool_.push_back(p.a);
+            pool_.push_back(p.b);
+        }
+        pending_.clear();
+    }
+    void clear() { totals_.clear(); }
+    // pcisph_kernel_time entries, name order; returns the number of kernels timed
+    int read(pcisph_kernel_time* out, int max_entries) const {
+        int n = 0;
+        for (auto& kv : totals_) {
+            if (out && n < max_entries) {
+                std::memset(out[n].name, 0, sizeof(out[n].name));
+                std::strncpy(out[n].name, kv.first.c_str(), sizeof(out[n].name) - 1);
+                out[n].launches = kv.second.launches;
+                out[n].total_ms = kv.second.ms;
+            }
+            ++n;
+        }
+        return n;
+    }
+    // destroys the events (call with the owner's device current); the timer stays usable
+    void release() {
+        for (auto& p : pending_) {
+            cudaEventDestroy(p.a);
+            cudaEventDestroy(p.b);
+        }
+        for (auto e : pool_) cudaEventDestroy(e);
+        pending_.clear();
+        pool_.clear();
+    }
+    ~KernelTimer() { release(); }
+
+   private:
+    struct Pending {
+        std::string name;
+        cudaEvent_t a, b;
+    };
+    cudaEvent_t take() {
+        if (!pool_.empty()) {
+            cudaEvent_t e = pool_.back();
+            pool_.pop_back();
+            return e;
+        }
+        cudaEvent_t e;
+        cudaEventCreate(&e);
+        return e;
+    }
+    std::map<std::string, Total> totals_;
+    std::vector<Pending> pending_;
+    std::vector<cudaEvent_t> pool_;
+};
 
 // Fluid.cpp:125-133
 inline uint32_t sort_bit_count_ref(uint32_t elements) {

@@ -178,3 +178,29 @@ def test_batch_bounded_sync():
     assert e.value.code == ERR_TIMEOUT
     bt.sync(timeout_ms=600000)
     assert all(bt.stats(i).steps == 101 for i in ids)
+
+
+@pytest.mark.parametrize("mode", [0, 2])
+def test_profiled_batch_steps_match_graph_steps(mode):
+    """Profiled batch steps (host-driven, every launch timed) compute the graph's bits and time every kernel."""
+    sc = _mixed_scenes()
+    out = []
+    for prof in (False, True):
+        bt = Batch(0, max_particles=sum(s.fluid_count for s in sc), max_scenes=len(sc), loop_mode=mode)
+        ids = [bt.add_scene(s) for s in sc]
+        bt.step(2)
+        if prof:
+            bt.profile(True)
+        bt.step(4)
+        bt.sync()
+        if prof:
+            t = bt.profile_read()
+            bt.profile(False)
+            want = {"hash", "radix_sort", "reorder", "density", "normal", "force"} | (
+                {"corrective_loop"} if mode == 2 else {"pressure", "decide", "pressure_force"})
+            assert want <= set(t), t
+            assert t["density"][0] == 4 and all(ms > 0 for _, ms in t.values())
+        out.append([_in_batch(bt, i, s) for i, s in zip(ids, sc)])
+        bt.close()
+    for s, a, b in zip(sc, out[0], out[1]):
+        _assert_same(s.name, b, a)
