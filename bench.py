@@ -66,7 +66,9 @@ WORKLOAD = ("dam break 128x128x64 = 1,048,576 particles, d=0.005 m, dt=2.5e-4 s,
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--steps", type=int, default=None,
+                    help="timed steps (default: the workload's own length -- dam1m 500, dam32k 1000, dam8m 200; "
+                         "scenes 200, bounding the one-context-per-scene comparison to about a minute)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=20.0, help="bound of the CPU baseline sample")
@@ -86,7 +88,10 @@ def parse():
                     help="corrective loop: 0 graph WHILE node, 2 persistent cooperative kernel")
     ap.add_argument("--spatial-order", type=int, default=2, choices=[0, 1, 2],
                     help="pcisph_options.spatial_order of the dam-break workloads (2: the library's choice)")
-    return ap.parse_args()
+    args = ap.parse_args()
+    if args.steps is None:
+        args.steps = {"dam1m": 500, "dam32k": 1000, "dam8m": 200, "scenes": 200}.get(args.workload, 200)
+    return args
 
 
 def max_over_ranks(x):
