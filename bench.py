@@ -55,6 +55,10 @@ DAM_WORKLOADS = {
     "dam32k": ("config0", "particle-steps/s @32K (<=1% rho err)",
                "dam break 32^3 = 32,768 particles, d=0.02 m, dt=1e-3 s, reflecting walls, "
                "3-50 corrective iterations to <1% density error"),
+    "dam1m_boundary": ("config1_boundary", "particle-steps/s @1M with 284K boundary particles (3-7 iterations)",
+                       "dam break 128x128x64 = 1,048,576 particles against 284,192 boundary particles (2 layers "
+                       "lining a 1.28x0.96x0.32 m box), d=0.005 m, dt=2.5e-4 s, reflecting walls, the reference's "
+                       "3-7 corrective iterations (threshold 1%)"),
     "dam8m": ("config2", "particle-steps/s @8M (<=1% rho err)",
               "two 256x128x128 blocks = 8,388,608 particles, d=0.0025 m, dt=1.25e-4 s, reflecting walls, "
               "3-50 corrective iterations to <1% density error"),
@@ -73,7 +77,8 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=20.0, help="bound of the CPU baseline sample")
     ap.add_argument("--variant", type=int, default=2, help="neighbour-sweep kernel variant (pcisph_options)")
-    ap.add_argument("--workload", default="dam1m", choices=["dam1m", "dam32k", "dam8m", "scenes", "serve"],
+    ap.add_argument("--workload", default="dam1m",
+                    choices=["dam1m", "dam1m_boundary", "dam32k", "dam8m", "scenes", "serve"],
                     help="dam1m: the 1M-particle dam break (the headline); dam32k / dam8m: the 32K and 8M "
                          "dam breaks; scenes: 256 scenes batched vs "
                          "stepped one context each; serve: Poisson requests through the serving loop")
@@ -90,7 +95,8 @@ def parse():
                     help="pcisph_options.spatial_order of the dam-break workloads (2: the library's choice)")
     args = ap.parse_args()
     if args.steps is None:
-        args.steps = {"dam1m": 500, "dam32k": 1000, "dam8m": 200, "scenes": 200}.get(args.workload, 200)
+        args.steps = {"dam1m": 500, "dam1m_boundary": 500, "dam32k": 1000, "dam8m": 200,
+                      "scenes": 200}.get(args.workload, 200)
     return args
 
 
@@ -207,22 +213,28 @@ def walk_candidates(f):
     return float(total.mean()) if total.size else 0.0
 
 
-def cpu_step_rate(scene, pos, vel, seconds, max_steps=None):
-    """Oracle steps from (pos, vel) until `seconds` of step time; returns (particle-steps/s, steps, iters)."""
-    import numpy as np
-
+def _oracle_for(scene):
+    """The oracle, the scene's parameters (boundary particles included) and step options."""
     from oracle.oracle import get as get_oracle
     from oracle.oracle import make_options
     O = get_oracle()
-    p = O.derive_params(scene.particle_radius, scene.rest_density, scene.fluid_count, 0, scene.delta_t,
-                        scene.gravity, scene.viscosity_constant(), scene.surface_tension)
+    p = O.derive_params(scene.particle_radius, scene.rest_density, scene.fluid_count, scene.boundary_count,
+                        scene.delta_t, scene.gravity, scene.viscosity_constant(), scene.surface_tension)
     opts = make_options(threshold=scene.threshold, min_iters=scene.min_iters, max_iters=scene.max_iters,
                         walls=scene.walls, box_lo=scene.box_lo, box_hi=scene.box_hi, restitution=scene.restitution)
-    s = O.new_state(p, pos, vel)
+    return O, p, opts
+
+
+def cpu_step_rate(scene, pos, vel, seconds, max_steps=None):
+    """Oracle steps from (pos, vel) until `seconds` of step time; returns (particle-steps/s, steps, iters).
+    Boundary particles are sorted in the first step only, as the GPU context sorts them once."""
+    import numpy as np
+    O, p, opts = _oracle_for(scene)
+    s = O.new_state(p, pos, vel, scene.boundary_pos)
     t_total, steps, iters = 0.0, 0, []
     while t_total < seconds and (max_steps is None or steps < max_steps):
         t0 = time.perf_counter()
-        st = O.step(p, opts, s)
+        st = O.step(p, opts, s, boundary_sort=steps == 0)
         t_total += time.perf_counter() - t0
         steps += 1
         iters.append(st.iterations)
@@ -232,23 +244,19 @@ def cpu_step_rate(scene, pos, vel, seconds, max_steps=None):
 def cpu_sample_rate(scene, states, seconds, max_steps=None):
     """Oracle steps from each of `states` ((pos, vel) at evenly spaced points of a run) in rounds, one step
     per state per round, until `seconds` of step time or `max_steps` steps (the run's length: each state
-    then covers its own segment of the run); returns (particle-steps/s, steps, mean iterations)."""
+    then covers its own segment of the run); returns (particle-steps/s, steps, mean iterations). Each run
+    sorts the boundary particles in its first step (included in the time: ~2% at 284K boundary particles)."""
     import numpy as np
-
-    from oracle.oracle import get as get_oracle
-    from oracle.oracle import make_options
-    O = get_oracle()
-    p = O.derive_params(scene.particle_radius, scene.rest_density, scene.fluid_count, 0, scene.delta_t,
-                        scene.gravity, scene.viscosity_constant(), scene.surface_tension)
-    opts = make_options(threshold=scene.threshold, min_iters=scene.min_iters, max_iters=scene.max_iters,
-                        walls=scene.walls, box_lo=scene.box_lo, box_hi=scene.box_hi, restitution=scene.restitution)
-    runs = [O.new_state(p, pos, vel) for pos, vel in states]
+    O, p, opts = _oracle_for(scene)
+    runs = [O.new_state(p, pos, vel, scene.boundary_pos) for pos, vel in states]
+    first = [True] * len(runs)
     t_total, steps, iters = 0.0, 0, []
     while t_total < seconds and (max_steps is None or steps < max_steps):
-        for s in runs:
+        for k, s in enumerate(runs):
             t0 = time.perf_counter()
-            st = O.step(p, opts, s)
+            st = O.step(p, opts, s, boundary_sort=first[k])
             t_total += time.perf_counter() - t0
+            first[k] = False
             steps += 1
             iters.append(st.iterations)
             if t_total >= seconds or (max_steps is not None and steps >= max_steps):

@@ -110,7 +110,7 @@ struct pcisph_ctx {
         return ListBuffers{b.pos, b.vel, b.pr4, b.normal, b.f_other, b.f_press, b.pred, b.pf4, b.state_pos,
                            b.state_vel, b.rho, b.press, b.err, w ? cells_w : b.cells, b.b_cells, b.b_pos, b.bpf,
                            b.nbr, b.nbr_count, b.near, b.near_count, b.bucket_fast, P.fluid_count,
-                           w ? d_of_w : nullptr, b.b_init, b.b_press};
+                           w ? d_of_w : nullptr, b.b_init, b.b_press, b.b_near};
     }
 
     // Working-order buffers for n particles and bk buckets; the index maps start as the identity.
@@ -195,7 +195,7 @@ struct pcisph_ctx {
         const size_t n = params.fluid_count;
         if (n >= (1u << 31)) return fail(PCISPH_ERR_INVALID_ARG, "kernel variant 2 takes fewer than 2^31 particles");
         const size_t bytes = align256(n * P.list_cap * 4) + align256(n * 4) + align256(n * P.near_cap * 4) +
-                             align256(n * 4) + align256(params.bucket_count);
+                             align256(n * 4) + align256(params.bucket_count) + align256(n);
         if (list_block.p && list_block.cap >= bytes && list_n == n) return PCISPH_OK;
         CUDA_TRY(cudaStreamSynchronize(stream()));
         if (list_block.ensure(bytes) != cudaSuccess)
@@ -206,6 +206,7 @@ struct pcisph_ctx {
         b.near = c.take<uint32_t>(n * P.near_cap);
         b.near_count = c.take<uint32_t>(n);
         b.bucket_fast = c.take<unsigned char>(params.bucket_count);
+        b.b_near = c.take<unsigned char>(n);
         list_n = n;
         graph_valid = false;
         order_age = kNoOrder;

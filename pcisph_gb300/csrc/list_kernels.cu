@@ -176,8 +176,16 @@ __global__ void __launch_bounds__(kBlock) k_density_list(PS ps, ListBuffers b) {
     const float4 xi = b.pos[i];
     const Cell c = cell_of(xi.x, xi.y, xi.z, P);
     float acc = 0.f;
-    if (P.boundary_count)
-        for_each_neighbour(b.b_cells, c, P, [&](uint32_t j) { acc += density_term(xi.x, xi.y, xi.z, __ldg(&b.b_pos[j]), P.h2); });
+    if (P.boundary_count) {
+        bool near_b = false;  // some boundary particle within r_list: the later sweeps must walk the boundary
+        for_each_neighbour(b.b_cells, c, P, [&](uint32_t j) {
+            const float4 o = __ldg(&b.b_pos[j]);
+            const float r2 = dist2(xi.x - o.x, xi.y - o.y, xi.z - o.z);
+            acc += poly6(r2, P.h2);  // density_term's expression
+            near_b |= r2 <= P.list_r2;
+        });
+        b.b_near[i] = near_b ? 1 : 0;
+    }
     const uint32_t stride = b.nbr_stride;
     uint32_t n = 0, nn = 0;
     __shared__ uint32_t staged[2][8 * kBlock];  // current chunk of each thread's skin and within-h lists
@@ -266,10 +274,17 @@ __device__ __forceinline__ float pressure_body(const PS& ps, const ListBuffers& 
         float acc = 0.f;
         const uint32_t cnt = b.nbr_count[i];
         const bool overflow = cnt > P.list_cap;
+        // boundary terms: all zero unless a boundary particle was within r_list of x, or x* moved more than
+        // half the skin from x (boundary particles do not move)
+        bool walk_boundary = false;
+        if (P.boundary_count) {
+            const float dx = xp.x - xi.x, dy = xp.y - xi.y, dz = xp.z - xi.z;
+            walk_boundary = b.b_near[i] != 0 || sqrtf(dist2(dx, dy, dz)) > P.list_half_skin;
+        }
         Cell c{0u, 0u, 0u};  // the cell (three IEEE divisions) only where a walk may need it
-        if (overflow || !all_lists_ok || P.boundary_count) c = cell_of(xi.x, xi.y, xi.z, P);
+        if (overflow || !all_lists_ok || walk_boundary) c = cell_of(xi.x, xi.y, xi.z, P);
         const bool walk = overflow || (!all_lists_ok && near_fast(P, b.bucket_fast, c));
-        if (P.boundary_count)
+        if (walk_boundary)
             for_each_neighbour(b.b_cells, c, P, [&](uint32_t j) { acc += density_term(xp.x, xp.y, xp.z, __ldg(&b.b_pos[j]), P.h2); });
         auto f = [&](uint32_t j) { acc += density_term(xp.x, xp.y, xp.z, __ldg(&b.pred[j]), P.h2); };
         if (walk) for_each_neighbour(b.cells, c, P, f);
@@ -330,9 +345,11 @@ __device__ __forceinline__ void pressure_force_body(const PS& ps, const ListBuff
     const float4 xi = b.pf4[i];
     float3 f = make_float3(0.f, 0.f, 0.f);
     const uint32_t cnt = b.near_count[i];
+    // boundary terms at x (within h): all zero unless a boundary particle was within r_list of x
+    const bool walk_boundary = P.boundary_count && b.b_near[i] != 0;
     Cell c{0u, 0u, 0u};
-    if (cnt > P.near_cap || P.boundary_count) c = cell_of(xi.x, xi.y, xi.z, P);
-    if (P.boundary_count)
+    if (cnt > P.near_cap || walk_boundary) c = cell_of(xi.x, xi.y, xi.z, P);
+    if (walk_boundary)
         for_each_neighbour(b.b_cells, c, P, [&](uint32_t j) { pressure_force_term(xi, __ldg(&b.bpf[j]), P.h, P.h2, f); });
     auto body = [&](uint32_t j) { pressure_force_term(xi, __ldg(&b.pf4[j]), P.h, P.h2, f); };
     if (cnt <= P.near_cap) for_each_listed(b.near, i, cnt, b.nbr_stride, body);

@@ -25,6 +25,8 @@ struct ListBuffers {
     const uint32_t* out_index;   // integration writes particle i's state at out_index[i] (null: at i)
     const float* b_init;         // boundary initial (self) densities and pressures (single scene, B > 0)
     float* b_press;
+    unsigned char* b_near;       // per fluid particle (B > 0): a boundary particle within r_list of x at the
+                                 // step's start; 0: the boundary terms of the step's sweeps are all zero
 };
 
 // One scene: parameters by value; the pressure kernel's last block decides the loop.

@@ -29,6 +29,7 @@ struct StepBuffers {
     uint32_t* near;                  // within-h lists, near_cap entries per particle
     uint32_t* near_count;            // entries per particle; > near_cap means "walk the buckets"
     unsigned char* bucket_fast;      // per bucket: holds a particle predicted to move > skin / 2 (this step)
+    unsigned char* b_near;           // per particle (B > 0): a boundary particle within the list radius
     // boundary
     float4 *b_pos, *bpf;
     float *b_press, *b_init;

@@ -609,3 +609,38 @@ def test_sweep_block_size_changes_no_result(block):
     for n in out[0][0]:
         np.testing.assert_array_equal(out[1][0][n], out[0][0][n], err_msg=n)
     assert out[0][1] == out[1][1]
+
+
+@pytest.mark.parametrize("variant", [1, 2])
+def test_boundary_scene_step_error_vs_fp64(oracle, variant):
+    """A fluid block inside a boundary box with room around it, some particles thrown at the walls: most
+    particles have no boundary particle within the list radius (variant 2 skips their boundary walks),
+    the thrown ones move more than half the skin in their predictions (they walk). Two steps of 5
+    iterations: the GPU's error against the FP64 rerun is of the order of the FP32 oracle's."""
+    d = 0.02
+    pos = scenes.lattice_block(10, 12, 10, d, (3 * d, 0.0, 3 * d), seed=9)
+    b_pos = scenes.boundary_box((0.0, 0.0, 0.0), (16 * d, 20 * d, 16 * d), d, layers=2)
+    rng = np.random.default_rng(9)
+    vel = (rng.standard_normal(pos.shape) * 0.05).astype(np.float32)
+    fast = rng.choice(pos.shape[0], 40, replace=False)
+    vel[fast] = (rng.standard_normal((40, 3)) * 4.0).astype(np.float32)  # > half the skin per step
+    n, nb = pos.shape[0], b_pos.shape[0]
+    p = oracle.derive_params(0.5 * d, 1000.0, n, nb, 1e-3, -9.81, 0.2 * d ** 3, 0.5)
+    opts = make_options(threshold=0.01, min_iters=5, max_iters=5, walls=False)
+    s32 = oracle.new_state(p, pos, vel, b_pos)
+    s64 = oracle.new_state(p, pos, vel, b_pos, dtype=np.float64)
+    f = fluid_like(p, min_iters=5, max_iters=5, kernel_variant=variant)
+    f.set_fluid_state(pos, vel)
+    f.set_boundary_state(b_pos)
+    for k in range(2):
+        oracle.step(p, opts, s32, boundary_sort=k == 0)
+        oracle.step(p, opts, s64, boundary_sort=k == 0)
+        f.update()
+    st = f.stats()
+    assert st.iterations == 5 and (variant == 1 or st.fast_particles > 0)
+    np.testing.assert_array_equal(f.get_field("src"), s64["f_src"])
+    for name, key in [("density", "f_rho"), ("pressure", "f_press"), ("position", "f_pos"), ("velocity", "f_vel"),
+                      ("boundary_pressure", "b_press")]:
+        e_gpu = rel_err(f.get_field(name), s64[key])
+        e_cpu = rel_err(s32[key], s64[key])
+        assert e_gpu <= 10 * e_cpu + 1e-6, (name, e_gpu, e_cpu)
