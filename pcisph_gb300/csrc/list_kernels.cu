@@ -21,7 +21,11 @@
 //     last for the rest of the step;
 //   - a particle with more than list_cap (near_cap) candidates is marked (count > cap) and walks the
 //     buckets in the sweeps that would use that list.
-// Boundary particles (B > 0, single scene) are summed by walking the boundary buckets.
+// Boundary particles (B > 0, single scene) are summed by walking the boundary buckets. The density sweep
+// records per particle whether any boundary particle lies within r_list of x (b_near); boundary particles
+// do not move, so a particle without one has only zero boundary terms in the pressure-force sweep (pairs
+// within h of x) and, unless its prediction moved more than half the skin, in the pressure sweeps: those
+// skip the boundary walk (27 bucket lookups and the hash-colliding boundary particles they hold).
 //
 // Parameter sources (list_kernels.cuh): OneScene passes one DevParams by value and the pressure kernel's
 // last block decides the loop. SceneTable serves a batch: particle i belongs to scene scene_of[i], whose
