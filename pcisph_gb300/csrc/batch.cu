@@ -624,7 +624,7 @@ int pcisph_batch_autotune(pcisph_batch* b, uint32_t steps, pcisph_batch_tune_res
     int best_mode = entry_mode, best_bits = entry_bits, cands = 1;
     const float skins[] = {0.2f, 0.25f, 0.3f};
     const int modes[] = {0, 2};
-    const int bits[] = {8, 6};
+    const int bits[] = {8, 10, 6};
     for (float sk : skins)
         for (int md : modes)
             for (int bt : bits) {

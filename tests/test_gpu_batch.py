@@ -156,7 +156,7 @@ def test_batch_autotune_leaves_results_unchanged():
         bt.step(2)
         if tune:
             r = bt.autotune(steps=1)
-            assert r["candidates"] == 12 and r["ms_per_step"] <= r["ms_per_step_before"]
+            assert r["candidates"] == 18 and r["ms_per_step"] <= r["ms_per_step_before"]
         bt.step(4)
         bt.sync()
         out.append([_in_batch(bt, i, s) for i, s in zip(ids, sc)])

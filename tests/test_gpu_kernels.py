@@ -492,7 +492,7 @@ def test_autotune_leaves_the_simulation_unchanged():
         f.step(3)
         if tune:
             r = f.autotune(steps=2)
-            assert r["candidates"] == 18 and r["ms_per_step"] <= r["ms_per_step_before"]
+            assert r["candidates"] == 26 and r["ms_per_step"] <= r["ms_per_step_before"]
             assert f.get_options().list_skin == pytest.approx(r["list_skin"])
             assert f.get_options().sweep_block == r["sweep_block"] in (128, 256, 512)
         f.step(5)
@@ -644,3 +644,19 @@ def test_boundary_scene_step_error_vs_fp64(oracle, variant):
         e_gpu = rel_err(f.get_field(name), s64[key])
         e_cpu = rel_err(s32[key], s64[key])
         assert e_gpu <= 10 * e_cpu + 1e-6, (name, e_gpu, e_cpu)
+
+
+def test_rederive_after_autotune_keeps_a_valid_sort_scratch():
+    """Parameters changed after autotuning re-derive the scene (and the default sort digit width): the next
+    steps still sort, with a scratch sized for that width."""
+    from pcisph_gb300 import setup_scene
+    sc = scenes.batch_drop(6000, d=0.01, seed=15)
+    f = Fluid(0)
+    setup_scene(f, sc)
+    f.step(2)
+    f.autotune(steps=1)
+    f.set_viscosity(sc.viscosity_constant() * 1.5)  # re-derives at the next update
+    f.step(3)
+    st = f.stats()
+    assert st.steps == 5 and (st.status_all & 4) == 0
+    f.close()
