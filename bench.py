@@ -40,7 +40,7 @@ ALGO_BYTES = {
     "pressure_force": 72,   # x 12 + p 4 + rho 4 + cell table 4 + F_p 12; predict: v 12, F_o 12, x* 12
     "reorder": 60,          # keys 4 + ids 4 + x, v gathered 24 + x, v written 24 + table 4
     "hash": 20,             # x 12 + key 4 + id 4
-    "radix_sort": 48,       # 3 passes of 8 B read + 8 B written
+    "radix_sort": 32,       # 2 passes (10-bit digits for the 19-bit keys at 1M) of 8 B read + 8 B written
 }
 # compulsory bytes of a whole step per particle: 340 + 136 per corrective iteration (hash 20, 3 sort passes
 # 60, cell reset 4, reorder 60, density 20, normal 32, force 72, integrate 72; per iteration predict 60,
