@@ -5,7 +5,7 @@
 // and the subset within h (plus a 1e-4 relative margin, far above rounding). The later sweeps of the step
 // iterate a list instead of walking the buckets again: the sweeps at the current positions (normal,
 // force, pressure force) the within-h list (~34 candidates), the pressure sweeps of the corrective
-// iterations the skin list (~65), instead of the walk's ~300. Because a list keeps the walk order and
+// iterations the skin list (~65-80), instead of the walk's ~210. Because a list keeps the walk order and
 // drops only pairs that contribute exactly zero, the sums are the reference's sums in the reference's
 // order.
 //
