@@ -91,6 +91,8 @@ def parse():
                     help="run the library's autotuner on the warmed-up state before timing (results unchanged)")
     ap.add_argument("--loop-mode", type=int, default=0, choices=[0, 2],
                     help="corrective loop: 0 graph WHILE node, 2 persistent cooperative kernel")
+    ap.add_argument("--list-skin", type=float, default=None,
+                    help="pcisph_options.list_skin of the dam-break workloads (default: the library's 0.25)")
     ap.add_argument("--spatial-order", type=int, default=2, choices=[0, 1, 2],
                     help="pcisph_options.spatial_order of the dam-break workloads (2: the library's choice)")
     args = ap.parse_args()
@@ -540,6 +542,8 @@ def main():
     torch.cuda.set_stream(stream)
     f = Fluid(local, stream=stream.cuda_stream)
     setup_scene(f, sc, kernel_variant=args.variant, loop_mode=args.loop_mode, spatial_order=args.spatial_order)
+    if args.list_skin is not None:
+        f.set_options(list_skin=args.list_skin)
     sampler = ClockSampler(local)
     sampler.start()
     for _ in range(args.warmup):
