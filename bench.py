@@ -192,6 +192,27 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
+def host_link_rates(nbytes, reps=10):
+    """Pinned host <-> device copy rates (GB/s) for nbytes, the bound of the e2e copies."""
+    import torch
+    h = torch.empty(nbytes, dtype=torch.uint8).pin_memory()
+    d = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    for _ in range(3):
+        d.copy_(h, non_blocking=True)
+        h.copy_(d, non_blocking=True)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        d.copy_(h, non_blocking=True)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    for _ in range(reps):
+        h.copy_(d, non_blocking=True)
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    return {"h2d": reps * nbytes / (t1 - t0) / 1e9, "d2h": reps * nbytes / (t2 - t1) / 1e9}
+
+
 def walk_candidates(f):
     """Mean candidates per particle of the reference's 27-bucket walk (grid_utils.cl:65-79) at the last
     step's sorted positions: the pair evaluations each of its neighbour sweeps makes per particle."""
@@ -632,7 +653,8 @@ def main():
     e2e_s = time.perf_counter() - t0 - t_copy
     e2e = {"value": N * e2e_steps * world / e2e_s, "unit": "particle-steps/s", "h2d_bytes_per_step": 24 * N,
            "d2h_bytes_per_step": 24 * N, "steps": e2e_steps,
-           "device_value_same_steps": N * e2e_steps * world / (sum(step_ms[:e2e_steps]) / 1e3)}
+           "device_value_same_steps": N * e2e_steps * world / (sum(step_ms[:e2e_steps]) / 1e3),
+           "host_link_GBps": host_link_rates(24 * N)}
 
     cand = walk_candidates(f)
     step_bytes = STEP_FIXED_BYTES + STEP_ITER_BYTES * iters
