@@ -132,9 +132,9 @@ def peaks():
         return 6800.0, "fallback"
 
 
-def ncu_traffic(variant):
-    """Per-kernel DRAM bytes per particle of one kernel variant, from the committed ncu summary
-    (profiles/ncu_traffic.txt)."""
+def ncu_records(variant):
+    """Per-kernel ncu figures of one kernel variant from the committed summary (profiles/ncu_traffic.txt):
+    {kernel: {"dram_bytes_per_particle": ..., "l1tex_throughput_active_pct": ..., ...}}."""
     out = {}
     path = os.path.join(ROOT, "profiles", "ncu_traffic.txt")
     if not os.path.exists(path):
@@ -144,8 +144,26 @@ def ncu_traffic(variant):
             if line.startswith("kernel="):
                 kv = dict(tok.split("=", 1) for tok in line.split())
                 if int(kv.get("variant", -1)) == variant:
-                    out[kv["kernel"]] = float(kv["dram_bytes_per_particle"])
+                    out[kv["kernel"]] = {k: float(v) for k, v in kv.items()
+                                         if k not in ("kernel", "variant", "source")}
     return out
+
+
+def binding_unit(variant, kernel):
+    """The unit that bounds a neighbour sweep by its committed ncu capture: the list sweeps gather ~24
+    sectors per warp request and keep the L1 data pipe busy, not HBM."""
+    r = ncu_records(variant).get(kernel, {})
+    if "l1tex_throughput_active_pct" not in r:
+        return None
+    return {"unit": "L1/tex (gather wavefronts)", "busy_frac_while_active": r["l1tex_throughput_active_pct"] / 100.0,
+            "issue_busy_frac": r.get("issue_active_pct", 0.0) / 100.0,
+            "source": "profiles/ncu_traffic.txt (ncu --set full of the same kernel)"}
+
+
+def ncu_traffic(variant):
+    """Per-kernel DRAM bytes per particle of one kernel variant (profiles/ncu_traffic.txt)."""
+    return {k: r["dram_bytes_per_particle"] for k, r in ncu_records(variant).items()
+            if "dram_bytes_per_particle" in r}
 
 
 class ClockSampler:
@@ -693,7 +711,8 @@ def main():
                          "frac": achieved / peak, "peak_kind": peak_kind,
                          "traffic": traffic * N if traffic else None,
                          "algo_bytes_per_particle": algo.get(dname, 0), "avg_launch_us": avg_s * 1e6,
-                         "profile_pass_iterations_per_step": prof_iters},
+                         "profile_pass_iterations_per_step": prof_iters,
+                         "binding_unit": binding_unit(args.variant, dname)},
             "kernels": kernels,
             "cpu_baseline": cpu,
             "clocks": clocks,
