@@ -71,8 +71,8 @@ def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=None,
-                    help="timed steps (default: the workload's own length -- dam1m 500, dam32k 1000, dam8m 200; "
-                         "scenes 200, bounding the one-context-per-scene comparison to about a minute)")
+                    help="timed steps (default: the workload's own length -- dam1m 500, dam32k 1000, dam8m 200, "
+                         "scenes 500)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=20.0, help="bound of the CPU baseline sample")
@@ -92,13 +92,14 @@ def parse():
     ap.add_argument("--loop-mode", type=int, default=0, choices=[0, 2],
                     help="corrective loop: 0 graph WHILE node, 2 persistent cooperative kernel")
     ap.add_argument("--list-skin", type=float, default=None,
-                    help="pcisph_options.list_skin of the dam-break workloads (default: the library's 0.25)")
+                    help="list skin in units of h: pcisph_options.list_skin of the dam-break workloads (default "
+                         "0.25), a fixed skin for the batched workloads (default: each scene adapts its own)")
     ap.add_argument("--spatial-order", type=int, default=2, choices=[0, 1, 2],
                     help="pcisph_options.spatial_order of the dam-break workloads (2: the library's choice)")
     args = ap.parse_args()
     if args.steps is None:
         args.steps = {"dam1m": 500, "dam1m_boundary": 500, "dam32k": 1000, "dam8m": 200,
-                      "scenes": 200}.get(args.workload, 200)
+                      "scenes": 500}.get(args.workload, 200)
     return args
 
 
@@ -373,6 +374,7 @@ def scenes_workload(args, rank, world, local):
 
     # batched: every scene in one pool, one graph launch per step
     bt = Batch(local, max_particles=n_total, max_scenes=len(sc), stream=stream.cuda_stream, loop_mode=args.loop_mode)
+    bt.set_list_skin("adaptive" if args.list_skin is None else args.list_skin)
     ids = [bt.add_scene(s) for s in sc]
     for _ in range(args.warmup):
         bt.step(1)
@@ -474,6 +476,7 @@ def scenes_workload(args, rank, world, local):
                        "scene_steps_per_s": len(all_sc) * args.steps / (ms_batch / 1e3),
                        "mean_scene_iterations": float(np.mean(iters)), "batch_loop_iterations": batch_loop_iters,
                        "loop_mode": args.loop_mode, "autotuned": tuned,
+                       "list_skin": "adaptive" if args.list_skin is None else args.list_skin,
                        "l2": "working set ~6 GB > L2"},
             "per_scene_contexts": {"value": n_all * args.steps / (ms_single / 1e3), "unit": "particle-steps/s",
                                    "ms_per_step": ms_single / args.steps, "gpu_launches": single_launches,
@@ -510,6 +513,7 @@ def serve_workload(args, rank, world, local):
     torch.cuda.set_stream(stream)
     bt = Batch(local, max_particles=max_particles, max_scenes=max_scenes, stream=stream.cuda_stream,
                loop_mode=args.loop_mode)
+    bt.set_list_skin("adaptive" if args.list_skin is None else args.list_skin)
     srv = Server(bt, budget, bpp, bps, max_particles, max_scenes, keep_state=True)
     # warm-up: one small request served to completion before the clock starts (graph build, first launches)
     Server(bt, budget, bpp, bps, max_particles, max_scenes, keep_state=False).run(reqs[:1], realtime=False)
@@ -539,6 +543,7 @@ def serve_workload(args, rank, world, local):
             "config": {"workload": SERVE_WORKLOAD, "rate_per_s": args.rate, "budget_gb": args.budget_gb,
                        "duration_s": args.duration, "requests_generated": horizon,
                        "offered_particle_steps_per_s": offered, "pool_particles": max_particles,
+                       "list_skin": "adaptive" if args.list_skin is None else args.list_skin,
                        "parallelism": f"requests sharded over {world} GPU(s)"},
             "serve": got if world > 1 else summ,
             "e2e": {"value": ps / wall, "unit": "particle-steps/s",

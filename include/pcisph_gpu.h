@@ -112,6 +112,8 @@ typedef struct pcisph_step_stats {
     uint64_t list_fallbacks;     /* variant 2: pressure sweeps in which some predicted displacement exceeded
                                     half the list skin (the particles near it walked the buckets) */
     uint64_t fast_particles;     /* variant 2: predictions that moved more than half the list skin */
+    float list_skin;             /* variant 2: the list skin of the last step, units of h */
+    uint32_t reserved;
 } pcisph_step_stats;
 
 /* ----------------------------------------------------------- enums */
@@ -310,8 +312,9 @@ PCISPH_API int pcisph_batch_add_scene(pcisph_batch* batch, const pcisph_scene_de
  * the pool once for all removals (stream-ordered device copies). */
 PCISPH_API int pcisph_batch_remove_scene(pcisph_batch* batch, int32_t scene_id);
 /* Autotuning of a batch on its current scenes: times `steps` batched steps (after a warm-up step) for each
- * list skin 0.2, 0.25, 0.3 x loop mode 0, 2 x radix digit width 8, 6, restoring the pool's state and
- * statistics after each, and keeps the fastest. Every candidate computes the same bits. Synchronises. */
+ * list skin (adaptive, 0.25, 0.35, 0.5) x loop mode 0, 2 x radix digit width 8, 10, 6, restoring the
+ * pool's state and statistics after each, and keeps the fastest. Every candidate computes the same bits.
+ * Synchronises. list_skin = PCISPH_LIST_SKIN_ADAPTIVE when the adaptive skin won. */
 typedef struct pcisph_batch_tune_result {
     float list_skin;
     int32_t loop_mode;
@@ -324,6 +327,12 @@ PCISPH_API int pcisph_batch_autotune(pcisph_batch* batch, uint32_t steps, pcisph
 /* 0 (default): the corrective loop is a conditional WHILE node of the step's graph; 2: one persistent
  * cooperative kernel runs it with per-scene convergence flags. Same results either way. */
 PCISPH_API int pcisph_batch_set_loop_mode(pcisph_batch* batch, int loop_mode);
+/* Neighbour-list skin of every scene, in units of h, in [0, 2] (pcisph_options.list_skin of a single
+ * context), or PCISPH_LIST_SKIN_ADAPTIVE (the default): before each step every scene takes the smallest of
+ * the skins 0.25, 0.35, 0.5 that at most 1 in 500 of its previous step's predictions outran (the largest
+ * if none), on the device. Results do not depend on the skin. */
+#define PCISPH_LIST_SKIN_ADAPTIVE (-1.0f)
+PCISPH_API int pcisph_batch_set_list_skin(pcisph_batch* batch, float skin);
 PCISPH_API int pcisph_batch_info(const pcisph_batch* batch, uint32_t* scenes, uint32_t* particles,
                                  uint32_t* free_particles);
 /* steps time steps of every scene (one CUDA graph launch each; no host synchronisation). */

@@ -17,6 +17,7 @@ OK, ERR_INVALID_ARG, ERR_OOM, ERR_CUDA, ERR_INCONSISTENT, ERR_NOT_READY, ERR_TIM
 STEP_NOT_CONVERGED, STEP_NONFINITE = 1, 2
 LAYOUT_PACKED3, LAYOUT_FLOAT4, LAYOUT_SCALAR = 0, 1, 2
 MEM_HOST, MEM_DEVICE = 0, 1
+LIST_SKIN_ADAPTIVE = -1.0  # pcisph_batch_set_list_skin: each scene picks its skin every step
 FIELDS = {
     "position": 0, "velocity": 1, "normal": 2, "predicted_position": 3, "density": 4, "other_force": 5,
     "pressure": 6, "pressure_force": 7, "density_variation": 8, "sorted_position": 9, "sorted_velocity": 10,
@@ -56,7 +57,8 @@ class Options(C.Structure):
 class StepStats(C.Structure):
     _fields_ = [("iterations", C.c_int32), ("max_density_error", C.c_float), ("status", C.c_uint32),
                 ("status_all", C.c_uint32), ("steps", C.c_uint64), ("total_iterations", C.c_uint64),
-                ("list_fallbacks", C.c_uint64), ("fast_particles", C.c_uint64)]
+                ("list_fallbacks", C.c_uint64), ("fast_particles", C.c_uint64), ("list_skin", C.c_float),
+                ("reserved", C.c_uint32)]
 
 
 class SceneDesc(C.Structure):
@@ -181,6 +183,7 @@ def load():
         "pcisph_batch_get_field": ([vp, C.c_int32, i32, vp, sz, i32, i32], i32),
         "pcisph_batch_set_state": ([vp, C.c_int32, vp, vp, C.c_uint32, i32, i32], i32),
         "pcisph_batch_set_loop_mode": ([vp, i32], i32),
+        "pcisph_batch_set_list_skin": ([vp, C.c_float], i32),
         "pcisph_batch_autotune": ([vp, C.c_uint32, C.POINTER(BatchTuneResult)], i32),
         "pcisph_batch_graph_stats": ([vp, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)], i32),
         "pcisph_batch_kernel_launches": ([vp], C.c_uint64),

@@ -88,13 +88,21 @@ class Batch:
         unchanged by any choice); returns the choice and the step times."""
         r = _lib.BatchTuneResult()
         check(self._L.pcisph_batch_autotune(self._h, int(steps), C.byref(r)))
-        return {"list_skin": r.list_skin, "loop_mode": r.loop_mode, "digit_bits": r.digit_bits,
+        skin = "adaptive" if r.list_skin == _lib.LIST_SKIN_ADAPTIVE else r.list_skin
+        return {"list_skin": skin, "loop_mode": r.loop_mode, "digit_bits": r.digit_bits,
                 "ms_per_step": r.ms_per_step, "ms_per_step_before": r.ms_per_step_before,
                 "candidates": r.candidates}
 
     def set_loop_mode(self, mode):
         """0: the corrective loop as a graph WHILE node; 2: one persistent cooperative kernel."""
         check(self._L.pcisph_batch_set_loop_mode(self._h, int(mode)))
+
+    def set_list_skin(self, skin):
+        """Neighbour-list skin of every scene in units of h, or "adaptive" (the default: each scene picks
+        0.25, 0.35 or 0.5 before each step from its previous step's displacements); results do not depend
+        on it."""
+        v = _lib.LIST_SKIN_ADAPTIVE if skin == "adaptive" else float(skin)
+        check(self._L.pcisph_batch_set_list_skin(self._h, v))
 
     def remove_scene(self, sid):
         check(self._L.pcisph_batch_remove_scene(self._h, int(sid)))

@@ -41,7 +41,7 @@ struct SceneSlot {
     bool removed;  // dropped at the next compaction
 };
 
-constexpr size_t kParticleBytes = 11 * 16 + 3 * 4 + 4 * 4 + 2 + (kListCap + kNearCap) * 4;  // allocate()'s arrays
+constexpr size_t kParticleBytes = 11 * 16 + 3 * 4 + 4 * 4 + 2 + (kListCapWide + kNearCap) * 4;  // allocate()'s arrays
 constexpr size_t kBucketBytesPerParticle = 5;  // (8 B table + 1 B flag) per bucket, ~N/2 buckets
 
 }  // namespace
@@ -69,7 +69,8 @@ struct pcisph_batch {
     uint32_t n_particles = 0, n_buckets = 0;
     int max_iters = 1;
     int loop_mode = 0;   // 0: conditional WHILE node; 2: one persistent cooperative kernel
-    float list_skin = 0.25f;
+    float list_skin = 0.25f;   // the skin of every scene when adaptive_skin is off
+    bool adaptive_skin = true;  // each scene picks its skin every step (k_batch_begin)
     bool dirty = false;  // scenes were added or removed since the tables were built
     cudaGraphExec_t graph_exec = nullptr;
     bool graph_valid = false;
@@ -104,7 +105,7 @@ struct pcisph_batch {
     int allocate() {
         const size_t n = max_particles, nb = max_buckets, ns = max_scenes;
         const size_t bytes = 11 * align256(n * 16) + 3 * align256(n * 4) + 4 * align256(n * 4) + align256(n * 2) +
-                             align256(n * kListCap * 4) + align256(n * kNearCap * 4) + align256(nb * 8) +
+                             align256(n * kListCapWide * 4) + align256(n * kNearCap * 4) + align256(nb * 8) +
                              align256(nb);
         if (pool.ensure(bytes) != cudaSuccess)
             return report_error(PCISPH_ERR_OOM, "device allocation of the batch pool failed (" + std::to_string(bytes) + " bytes)");
@@ -128,7 +129,7 @@ struct pcisph_batch {
         nbr_count = c.take<uint32_t>(n);
         near_count = c.take<uint32_t>(n);
         scene_of = c.take<uint16_t>(n);
-        nbr = c.take<uint32_t>(n * kListCap);
+        nbr = c.take<uint32_t>(n * kListCapWide);
         near = c.take<uint32_t>(n * kNearCap);
         cells = c.take<uint2>(nb);
         bucket_fast = c.take<unsigned char>(nb);
@@ -222,7 +223,8 @@ struct pcisph_batch {
             s.bucket_base = base;
             const pcisph_scene_desc& d = s.desc;
             make_devparams(s.params, d.min_iterations, d.max_iterations, d.walls, d.box_lo, d.box_hi, d.restitution,
-                           d.density_variation_threshold, list_skin, base, &table[k]);
+                           d.density_variation_threshold, adaptive_skin ? skin_level_value(0) : list_skin, base,
+                           &table[k], kListCapWide, adaptive_skin ? 1 : 0);
             offsets[k] = off;
             off += s.count;
             base += s.params.bucket_count;
@@ -248,7 +250,7 @@ struct pcisph_batch {
     int record_prefix(cudaStream_t s) {
         const SceneTable t = scene_table();
         int nl = 0;
-        launch_batch_begin(d_ctls, t.n_scenes, d_batch, s);
+        launch_batch_begin(d_table, d_ctls, t.n_scenes, d_batch, s);
         ++nl;
         if (cudaMemsetAsync(cells, 0, (size_t)n_buckets * 8, s) != cudaSuccess) return -1;
         if (cudaMemsetAsync(bucket_fast, 0, n_buckets, s) != cudaSuccess) return -1;
@@ -578,7 +580,7 @@ int pcisph_batch_autotune(pcisph_batch* b, uint32_t steps, pcisph_batch_tune_res
     BTRY(cudaMemcpyAsync(sc, b->d_ctls, (size_t)ns * sizeof(Control), cudaMemcpyDeviceToDevice, s));
     BTRY(cudaMemcpyAsync(sc + ns, b->d_batch, sizeof(Control), cudaMemcpyDeviceToDevice, s));
     const uint64_t launches0 = b->host_launches;
-    const float entry_skin = b->list_skin;
+    const float entry_skin = b->adaptive_skin ? PCISPH_LIST_SKIN_ADAPTIVE : b->list_skin;
     const int entry_mode = b->loop_mode, entry_bits = b->sorter.digit_bits();
     auto restore = [&]() -> int {
         BTRY(cudaMemcpyAsync(b->state_pos, sp, (size_t)n * 16, cudaMemcpyDeviceToDevice, s));
@@ -589,7 +591,8 @@ int pcisph_batch_autotune(pcisph_batch* b, uint32_t steps, pcisph_batch_tune_res
         return PCISPH_OK;
     };
     auto apply = [&](float skin, int mode, int bits) -> int {
-        b->list_skin = skin;
+        b->adaptive_skin = skin == PCISPH_LIST_SKIN_ADAPTIVE;
+        if (!b->adaptive_skin) b->list_skin = skin;
         b->loop_mode = mode;
         b->sorter.set_digit_bits(bits);
         b->sort_block.release();
@@ -622,7 +625,7 @@ int pcisph_batch_autotune(pcisph_batch* b, uint32_t steps, pcisph_batch_tune_res
     if (!rc) rc = time_it(&before);
     float best_ms = before, best_skin = entry_skin;
     int best_mode = entry_mode, best_bits = entry_bits, cands = 1;
-    const float skins[] = {0.2f, 0.25f, 0.3f};
+    const float skins[] = {PCISPH_LIST_SKIN_ADAPTIVE, 0.25f, 0.35f, 0.5f};
     const int modes[] = {0, 2};
     const int bits[] = {8, 10, 6};
     for (float sk : skins)
@@ -666,6 +669,18 @@ int pcisph_batch_set_loop_mode(pcisph_batch* b, int loop_mode) {
         b->graph_valid = false;
     }
     return PCISPH_OK;
+}
+
+int pcisph_batch_set_list_skin(pcisph_batch* b, float skin) {
+    if (!b) return report_error(PCISPH_ERR_INVALID_ARG, "batch is NULL");
+    if (!(skin == PCISPH_LIST_SKIN_ADAPTIVE || (skin >= 0.f && skin <= 2.f)))
+        return report_error(PCISPH_ERR_INVALID_ARG, "list_skin must be in [0, 2], or PCISPH_LIST_SKIN_ADAPTIVE");
+    const bool adaptive = skin == PCISPH_LIST_SKIN_ADAPTIVE;
+    if (adaptive == b->adaptive_skin && (adaptive || skin == b->list_skin)) return PCISPH_OK;
+    DeviceGuard g(b->device);
+    b->adaptive_skin = adaptive;
+    if (!adaptive) b->list_skin = skin;
+    return b->rebuild();  // scene tables with the new list radius
 }
 
 int pcisph_batch_info(const pcisph_batch* b, uint32_t* scenes, uint32_t* particles, uint32_t* free_particles) {
@@ -720,6 +735,8 @@ int pcisph_batch_scene_stats(pcisph_batch* b, int32_t id, pcisph_step_stats* out
     out->total_iterations = c.total_iters;
     out->list_fallbacks = c.list_fallbacks;
     out->fast_particles = c.fast_particles;
+    out->list_skin = b->adaptive_skin ? skin_level_value((int)c.skin_level) : b->list_skin;
+    out->reserved = 0;
     return PCISPH_OK;
 }
 

@@ -30,6 +30,10 @@ struct DevParams {
     uint32_t near_cap;  // entries of the within-h list
     float near_r2;      // within-h list radius^2: h^2 (1 + 1e-4), a margin far above rounding
     float list_r, list_r2, list_half_skin;
+    // batched scenes with an adaptive skin: each step picks one of kSkinLevels skins from the previous
+    // step's count of predictions past each level's half skin (skin_half[k])
+    int adaptive_skin;
+    float skin_half[3];
     // options
     int min_iters, max_iters, walls;
     float box_lo[3], box_hi[3], restitution, threshold;
@@ -53,7 +57,21 @@ struct Control {
     unsigned long long fast_particles;  // predictions that moved more than skin / 2 (each flags its bucket)
     unsigned int finished;       // batched scenes: the step is complete (no more corrective iterations)
     unsigned int any_running;    // batch control: some scene still iterates
+    unsigned int skin_level;     // adaptive skin: the level of the current step
+    unsigned long long over_level[3];  // adaptive skin: this step's predictions past each level's half skin
 };
+
+// List skins (units of h) an adaptive scene chooses from, smallest first.
+constexpr int kSkinLevels = 3;
+__host__ __device__ inline float skin_level_value(int k) { return k <= 0 ? 0.25f : k == 1 ? 0.35f : 0.5f; }
+
+// The list radius h (1 + skin) and half the skin, less a margin for the rounding of |x_i - x_j| and
+// |x* - x| (relative 1e-6 of h): a prediction within list_half_skin of x keeps every list exact.
+__host__ __device__ inline void set_list_skin(DevParams* d, float skin) {
+    d->list_r = d->h * (1.f + skin);
+    d->list_r2 = d->list_r * d->list_r;
+    d->list_half_skin = 0.5f * d->h * skin - 1e-6f * d->h;
+}
 
 __host__ __device__ inline void magic_for(uint32_t d, uint32_t* magic, uint32_t* shift) {
     uint32_t l = 0;

@@ -825,6 +825,8 @@ struct pcisph_ctx {
         out->total_iterations = host_ctl->total_iters;
         out->list_fallbacks = host_ctl->list_fallbacks;
         out->fast_particles = host_ctl->fast_particles;
+        out->list_skin = opts.list_skin;
+        out->reserved = 0;
         return PCISPH_OK;
     }
 

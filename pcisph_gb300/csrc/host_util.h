@@ -26,6 +26,8 @@ inline size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 inline constexpr float kPi = 3.14159265358979323846f;  // utils/constants.h:4
 inline constexpr uint32_t kListCap = 96;           // neighbour-list entries per particle (multiple of 4)
 inline constexpr uint32_t kNearCap = 64;           // within-h list entries per particle
+// skin-list entries per particle of a batch (skins up to 0.5 h: ~48 (1 + skin)^3 entries at rest density)
+inline constexpr uint32_t kListCapWide = 168;
 
 // Wait up to timeout_ms for the work queued on s (0: look once). *done = false when it is still running at
 // the deadline; the work is left queued and a later wait can pick it up.
@@ -239,7 +241,8 @@ struct Carver {
 // Kernel parameters of one scene from its reference parameters and step options.
 inline void make_devparams(const pcisph_sim_params& p, int min_iters, int max_iters, int walls, const float* box_lo,
                            const float* box_hi, float restitution, float threshold, float list_skin,
-                           uint32_t bucket_base, DevParams* d) {
+                           uint32_t bucket_base, DevParams* d, uint32_t list_cap = kListCap,
+                           int adaptive_skin = 0) {
     *d = DevParams{};
     d->particle_mass = p.particle_mass;
     d->rest_density = p.rest_density;
@@ -262,13 +265,12 @@ inline void make_devparams(const pcisph_sim_params& p, int min_iters, int max_it
     d->bucket_count = p.bucket_count;
     magic_for(p.bucket_count, &d->bk_magic, &d->bk_shift);
     d->bucket_base = bucket_base;
-    d->list_cap = kListCap;
+    d->list_cap = list_cap;
     d->near_cap = kNearCap;
     d->near_r2 = p.kernel_radius2 * 1.0001f;
-    d->list_r = p.kernel_radius * (1.f + list_skin);
-    d->list_r2 = d->list_r * d->list_r;
-    // half the skin, less a margin for the rounding of |x_i - x_j| and |x* - x| (relative 1e-6 of h)
-    d->list_half_skin = 0.5f * p.kernel_radius * list_skin - 1e-6f * p.kernel_radius;
+    set_list_skin(d, list_skin);
+    d->adaptive_skin = adaptive_skin;
+    for (int k = 0; k < kSkinLevels; ++k) d->skin_half[k] = 0.5f * p.kernel_radius * skin_level_value(k);
     d->min_iters = min_iters;
     d->max_iters = max_iters;
     d->walls = walls;

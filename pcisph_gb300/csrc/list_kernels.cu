@@ -53,6 +53,14 @@ __device__ __forceinline__ void warp_atomic_max(unsigned* addr, unsigned v) {
     if ((int)(threadIdx.x & 31) == __ffs(peers) - 1) atomicMax(addr, m);
 }
 
+// Add the number of this warp's lanes with pred set to *addr: one atomic per group of lanes sharing addr.
+__device__ __forceinline__ void warp_count(unsigned long long* addr, bool pred) {
+    const unsigned act = __activemask();
+    const unsigned peers = __match_any_sync(act, (unsigned long long)addr);
+    const unsigned c = __popc(__ballot_sync(peers, pred));
+    if (c && (int)(threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(addr, (unsigned long long)c);
+}
+
 // List layout: entries k = 8c .. 8c+7 of particle i (chunk c) are 32 contiguous bytes at uint4 offset
 // 2 (c * stride + i); chunks are column-major over particles. A warp's 32 consecutive particles read
 // chunk c as 1 KB of contiguous memory, and the builder writes whole 32-byte sectors.
@@ -119,8 +127,13 @@ __device__ __forceinline__ void note_displacement(const DevParams& P, Control* c
     const float dx = xs.x - xi.x, dy = xs.y - xi.y, dz = xs.z - xi.z;  // exact: xs and xi are close
     const float disp = sqrtf(dist2(dx, dy, dz));
     warp_atomic_max(&ctl->max_disp_bits, __float_as_uint(disp));
-    if (disp > P.list_half_skin) {
-        atomicAdd(&ctl->fast_particles, 1ull);
+    const bool fast = disp > P.list_half_skin;
+    warp_count(&ctl->fast_particles, fast);
+    if (P.adaptive_skin) {
+#pragma unroll
+        for (int k = 0; k < kSkinLevels; ++k) warp_count(&ctl->over_level[k], disp > P.skin_half[k]);
+    }
+    if (fast) {
         const Cell c = cell_of(xi.x, xi.y, xi.z, P);
         bucket_fast[P.bucket_base + hash_key(c.x, c.y, c.z, P)] = 1;
     }
@@ -495,9 +508,27 @@ __global__ void k_batch_decide(const DevParams* __restrict__ table, Control* ctl
 }
 
 // Batch step start: per-scene iteration state.
-__global__ void k_batch_begin(Control* ctls, uint32_t n_scenes, Control* batch) {
+// Per scene, before a step: reset the step's control fields. A scene with an adaptive skin takes the
+// smallest skin level that at most 1 in 500 of the previous step's predictions outran (the largest if
+// none), from that step's counts, and writes its list radius into the scene table; the builder and the
+// sweeps of this step read it there. Results do not depend on the choice.
+__global__ void k_batch_begin(DevParams* table, Control* ctls, uint32_t n_scenes, Control* batch) {
     for (uint32_t s = threadIdx.x; s < n_scenes; s += blockDim.x) {
         Control* c = &ctls[s];
+        DevParams* P = &table[s];
+        if (P->adaptive_skin) {
+            int level = 0;
+            if (c->steps) {
+                const unsigned long long preds =
+                    (unsigned long long)P->fluid_count * (unsigned long long)max(c->iterations_last, 1);
+                level = kSkinLevels - 1;
+                for (int k = kSkinLevels - 1; k >= 0; --k)
+                    if (c->over_level[k] * 500ull <= preds) level = k;
+            }
+            c->skin_level = (unsigned)level;
+            set_list_skin(P, skin_level_value(level));
+            for (int k = 0; k < kSkinLevels; ++k) c->over_level[k] = 0;
+        }
         c->iter = 0;
         c->done = 0;
         c->finished = 0;
@@ -597,8 +628,8 @@ cudaError_t launch_corrective_loop_scenes(const SceneTable& t, const ListBuffers
     return launch_loop(t, t.n, b, batch, max_iters, s);
 }
 
-void launch_batch_begin(Control* ctls, uint32_t n_scenes, Control* batch, cudaStream_t s) {
-    k_batch_begin<<<1, 256, 0, s>>>(ctls, n_scenes, batch);
+void launch_batch_begin(DevParams* table, Control* ctls, uint32_t n_scenes, Control* batch, cudaStream_t s) {
+    k_batch_begin<<<1, 256, 0, s>>>(table, ctls, n_scenes, batch);
 }
 void launch_scene_of(const uint32_t* offsets, uint32_t n_scenes, uint32_t n, uint16_t* scene_of, cudaStream_t s) {
     if (n) k_scene_of<<<grid_for(n), kBlock, 0, s>>>(offsets, n_scenes, n, scene_of);

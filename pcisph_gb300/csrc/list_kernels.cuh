@@ -67,7 +67,7 @@ void launch_pressure_list(const DevParams& P, Control* ctl, const ListBuffers& b
 void launch_pressure_force_list(const DevParams& P, Control* ctl, const ListBuffers& b, int mode,
                                 cudaGraphConditionalHandle cond, bool use_cond, int block, cudaStream_t s);
 
-void launch_batch_begin(Control* ctls, uint32_t n_scenes, Control* batch, cudaStream_t s);
+void launch_batch_begin(DevParams* table, Control* ctls, uint32_t n_scenes, Control* batch, cudaStream_t s);
 void launch_scene_of(const uint32_t* offsets, uint32_t n_scenes, uint32_t n, uint16_t* scene_of, cudaStream_t s);
 void launch_hash_scenes(const SceneTable& t, const float4* pos, uint32_t* keys, cudaStream_t s);
 void launch_density_scenes(const SceneTable& t, const ListBuffers& b, cudaStream_t s);

@@ -156,7 +156,7 @@ def test_batch_autotune_leaves_results_unchanged():
         bt.step(2)
         if tune:
             r = bt.autotune(steps=1)
-            assert r["candidates"] == 18 and r["ms_per_step"] <= r["ms_per_step_before"]
+            assert r["candidates"] == 24 and r["ms_per_step"] <= r["ms_per_step_before"]
         bt.step(4)
         bt.sync()
         out.append([_in_batch(bt, i, s) for i, s in zip(ids, sc)])
@@ -204,3 +204,31 @@ def test_profiled_batch_steps_match_graph_steps(mode):
         bt.close()
     for s, a, b in zip(sc, out[0], out[1]):
         _assert_same(s.name, b, a)
+
+
+def test_adaptive_skin_follows_the_displacements_and_changes_no_bits():
+    """A block thrown along the floor at 6 m/s moves 0.15 h per prediction (h = 0.04 m, dt = 1 ms), past
+    half of the 0.25 h skin: with the adaptive skin its scene widens its lists (0.35 h) while a scene at
+    rest keeps 0.25 h; every skin, fixed or adaptive, computes the same bits."""
+    thrown = scenes.small_dam(9, seed=21)
+    rest = scenes.small_dam(7, seed=22)
+    v_thrown = np.zeros_like(thrown.fluid_pos)
+    v_thrown[:, 0] = 6.0
+    out, skins = {}, []
+    for skin in ("adaptive", 0.25, 0.5):
+        bt = Batch(0, max_particles=thrown.fluid_count + rest.fluid_count, max_scenes=2)
+        bt.set_list_skin(skin)
+        a = bt.add_scene(thrown, vel=v_thrown)
+        b = bt.add_scene(rest)
+        for _ in range(8):
+            bt.step(5)
+            if skin == "adaptive":
+                skins.append((bt.stats(a).list_skin, bt.stats(b).list_skin))
+        bt.sync()
+        out[skin] = [_in_batch(bt, a, thrown), _in_batch(bt, b, rest)]
+        bt.close()
+    for skin in (0.25, 0.5):
+        _assert_same("thrown", out[skin][0], out["adaptive"][0])
+        _assert_same("rest", out[skin][1], out["adaptive"][1])
+    assert skins[0][0] > 0.25, skins
+    assert all(abs(r - 0.25) < 1e-6 for _, r in skins), skins

@@ -30,7 +30,8 @@ def test_drop_scene_has_pool_and_sphere():
 
 def test_batch_memory_model():
     per_particle, per_scene = memory_model()
-    assert 400 < per_particle < 1000 and per_scene > 0
+    # 11 float4 state and work arrays, scalars, 168 skin-list and 64 within-h list entries, buckets, sort
+    assert per_particle == 11 * 16 + 3 * 4 + 4 * 4 + 2 + (168 + 64) * 4 + 5 + 12 and per_scene > 0
 
 
 def test_parameter_sweep_variants_are_a_product():
