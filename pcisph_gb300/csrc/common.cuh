@@ -34,6 +34,7 @@ struct DevParams {
     // step's count of predictions past each level's half skin (skin_half[k])
     int adaptive_skin;
     float skin_half[3];
+    uint32_t skin_outrun_ratio;  // a level qualifies if at most 1 in this many predictions outran it
     // options
     int min_iters, max_iters, walls;
     float box_lo[3], box_hi[3], restitution, threshold;

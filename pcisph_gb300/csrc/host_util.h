@@ -28,6 +28,9 @@ inline constexpr uint32_t kListCap = 96;           // neighbour-list entries per
 inline constexpr uint32_t kNearCap = 64;           // within-h list entries per particle
 // skin-list entries per particle of a batch (skins up to 0.5 h: ~48 (1 + skin)^3 entries at rest density)
 inline constexpr uint32_t kListCapWide = 168;
+// adaptive skin: a level qualifies if at most 1 in this many of the last step's predictions outran it
+// (config-3 batch over 500 steps: 27.1, 27.0, 27.1, 27.3 s at 500, 3000, 20000, 10^6)
+inline constexpr uint32_t kSkinOutrunRatio = 500;
 
 // Wait up to timeout_ms for the work queued on s (0: look once). *done = false when it is still running at
 // the deadline; the work is left queued and a later wait can pick it up.
@@ -270,6 +273,7 @@ inline void make_devparams(const pcisph_sim_params& p, int min_iters, int max_it
     d->near_r2 = p.kernel_radius2 * 1.0001f;
     set_list_skin(d, list_skin);
     d->adaptive_skin = adaptive_skin;
+    d->skin_outrun_ratio = kSkinOutrunRatio;
     for (int k = 0; k < kSkinLevels; ++k) d->skin_half[k] = 0.5f * p.kernel_radius * skin_level_value(k);
     d->min_iters = min_iters;
     d->max_iters = max_iters;

@@ -509,9 +509,9 @@ __global__ void k_batch_decide(const DevParams* __restrict__ table, Control* ctl
 
 // Batch step start: per-scene iteration state.
 // Per scene, before a step: reset the step's control fields. A scene with an adaptive skin takes the
-// smallest skin level that at most 1 in 500 of the previous step's predictions outran (the largest if
-// none), from that step's counts, and writes its list radius into the scene table; the builder and the
-// sweeps of this step read it there. Results do not depend on the choice.
+// smallest skin level that at most 1 in skin_outrun_ratio of the previous step's predictions outran (the
+// largest if none), from that step's counts, and writes its list radius into the scene table; the builder
+// and the sweeps of this step read it there. Results do not depend on the choice.
 __global__ void k_batch_begin(DevParams* table, Control* ctls, uint32_t n_scenes, Control* batch) {
     for (uint32_t s = threadIdx.x; s < n_scenes; s += blockDim.x) {
         Control* c = &ctls[s];
@@ -523,7 +523,7 @@ __global__ void k_batch_begin(DevParams* table, Control* ctls, uint32_t n_scenes
                     (unsigned long long)P->fluid_count * (unsigned long long)max(c->iterations_last, 1);
                 level = kSkinLevels - 1;
                 for (int k = kSkinLevels - 1; k >= 0; --k)
-                    if (c->over_level[k] * 500ull <= preds) level = k;
+                    if (c->over_level[k] * (unsigned long long)P->skin_outrun_ratio <= preds) level = k;
             }
             c->skin_level = (unsigned)level;
             set_list_skin(P, skin_level_value(level));
