@@ -53,7 +53,7 @@ struct Control {
     unsigned long long total_iters;
     unsigned int guard_iters;    // loop iterations counted by the pressure-force kernel (bounds the graph loop)
     unsigned int n_groups;       // bucket runs listed by the reorder kernel this step
-    unsigned int max_disp_bits;  // float bits of max |x* - x| this step (neighbour-list validity)
+    unsigned int any_fast;       // some prediction this step moved more than half the list skin
     unsigned long long list_fallbacks;  // pressure sweeps in which some particle moved more than skin / 2
     unsigned long long fast_particles;  // predictions that moved more than skin / 2 (each flags its bucket)
     unsigned int finished;       // batched scenes: the step is complete (no more corrective iterations)

@@ -53,11 +53,14 @@ __device__ __forceinline__ void warp_atomic_max(unsigned* addr, unsigned v) {
     if ((int)(threadIdx.x & 31) == __ffs(peers) - 1) atomicMax(addr, m);
 }
 
-// Add the number of this warp's lanes with pred set to *addr: one atomic per group of lanes sharing addr.
+// Add the number of this warp's lanes with pred set to *addr: one atomic per group of lanes sharing addr,
+// none when no lane has pred.
 __device__ __forceinline__ void warp_count(unsigned long long* addr, bool pred) {
     const unsigned act = __activemask();
+    const unsigned set = __ballot_sync(act, pred);
+    if (!set) return;
     const unsigned peers = __match_any_sync(act, (unsigned long long)addr);
-    const unsigned c = __popc(__ballot_sync(peers, pred));
+    const unsigned c = __popc(set & peers);
     if (c && (int)(threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(addr, (unsigned long long)c);
 }
 
@@ -120,13 +123,13 @@ __device__ __forceinline__ void for_each_listed(const uint32_t* __restrict__ lis
     }
 }
 
-// After predicting x*_i (stored as xs): record the max displacement; a fast particle flags its bucket.
+// After predicting x*_i (stored as xs): a fast particle (moved more than half the skin) flags its bucket
+// and the step; the predictions past each adaptive skin level are counted.
 __device__ __forceinline__ void note_displacement(const DevParams& P, Control* ctl,
                                                   unsigned char* __restrict__ bucket_fast, const float4& xi,
                                                   const float4& xs) {
     const float dx = xs.x - xi.x, dy = xs.y - xi.y, dz = xs.z - xi.z;  // exact: xs and xi are close
     const float disp = sqrtf(dist2(dx, dy, dz));
-    warp_atomic_max(&ctl->max_disp_bits, __float_as_uint(disp));
     const bool fast = disp > P.list_half_skin;
     warp_count(&ctl->fast_particles, fast);
     if (P.adaptive_skin) {
@@ -134,6 +137,7 @@ __device__ __forceinline__ void note_displacement(const DevParams& P, Control* c
         for (int k = 0; k < kSkinLevels; ++k) warp_count(&ctl->over_level[k], disp > P.skin_half[k]);
     }
     if (fast) {
+        ctl->any_fast = 1u;  // the same value from every fast lane: no atomic needed
         const Cell c = cell_of(xi.x, xi.y, xi.z, P);
         bucket_fast[P.bucket_base + hash_key(c.x, c.y, c.z, P)] = 1;
     }
@@ -173,7 +177,7 @@ __device__ __forceinline__ void decide(const DevParams& P, Control* ctl) {
     ctl->done = done ? 1u : 0u;
     ctl->max_err_bits = 0;
     ctl->blocks_done = 0;
-    if (__uint_as_float(ctl->max_disp_bits) > P.list_half_skin) ctl->list_fallbacks += 1;
+    if (ctl->any_fast) ctl->list_fallbacks += 1;
     if (done) {
         if (!converged) ctl->status |= 1u;
         ctl->status_all |= ctl->status;
@@ -285,7 +289,7 @@ __device__ __forceinline__ float pressure_body(const PS& ps, const ListBuffers& 
         const DevParams& P = ps.params(i);
         Control* ctl = ps.control(i);
         // no particle of the scene moved more than half the skin: its lists are complete for x*
-        const bool all_lists_ok = __uint_as_float(ctl->max_disp_bits) <= P.list_half_skin;
+        const bool all_lists_ok = ctl->any_fast == 0u;
         const float4 xi = b.pos[i];
         const float4 xp = b.pred[i];
         float acc = 0.f;
@@ -533,7 +537,7 @@ __global__ void k_batch_begin(DevParams* table, Control* ctls, uint32_t n_scenes
         c->done = 0;
         c->finished = 0;
         c->max_err_bits = 0;
-        c->max_disp_bits = 0;
+        c->any_fast = 0;
         c->status = 0;
     }
     if (threadIdx.x == 0) {
