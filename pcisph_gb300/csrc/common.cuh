@@ -53,9 +53,10 @@ struct Control {
     unsigned long long total_iters;
     unsigned int guard_iters;    // loop iterations counted by the pressure-force kernel (bounds the graph loop)
     unsigned int n_groups;       // bucket runs listed by the reorder kernel this step
-    unsigned int any_fast;       // some prediction this step moved more than half the list skin
     unsigned long long list_fallbacks;  // pressure sweeps in which some particle moved more than skin / 2
     unsigned long long fast_particles;  // predictions that moved more than skin / 2 (each flags its bucket)
+    unsigned long long fast_at_begin;   // fast_particles when the step began: a larger count now means some
+                                        // prediction of this step outran the lists
     unsigned int finished;       // batched scenes: the step is complete (no more corrective iterations)
     unsigned int any_running;    // batch control: some scene still iterates
     unsigned int skin_level;     // adaptive skin: the level of the current step

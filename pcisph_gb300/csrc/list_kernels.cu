@@ -124,7 +124,9 @@ __device__ __forceinline__ void for_each_listed(const uint32_t* __restrict__ lis
 }
 
 // After predicting x*_i (stored as xs): a fast particle (moved more than half the skin) flags its bucket
-// and the step; the predictions past each adaptive skin level are counted.
+// and is counted (one atomic per warp that has one; no store otherwise: in a splash most predictions are
+// fast, and a flag stored by each of their warps measured slower than the counts alone); the predictions
+// past each adaptive skin level are counted.
 __device__ __forceinline__ void note_displacement(const DevParams& P, Control* ctl,
                                                   unsigned char* __restrict__ bucket_fast, const float4& xi,
                                                   const float4& xs) {
@@ -137,7 +139,6 @@ __device__ __forceinline__ void note_displacement(const DevParams& P, Control* c
         for (int k = 0; k < kSkinLevels; ++k) warp_count(&ctl->over_level[k], disp > P.skin_half[k]);
     }
     if (fast) {
-        ctl->any_fast = 1u;  // the same value from every fast lane: no atomic needed
         const Cell c = cell_of(xi.x, xi.y, xi.z, P);
         bucket_fast[P.bucket_base + hash_key(c.x, c.y, c.z, P)] = 1;
     }
@@ -177,7 +178,7 @@ __device__ __forceinline__ void decide(const DevParams& P, Control* ctl) {
     ctl->done = done ? 1u : 0u;
     ctl->max_err_bits = 0;
     ctl->blocks_done = 0;
-    if (ctl->any_fast) ctl->list_fallbacks += 1;
+    if (ctl->fast_particles != ctl->fast_at_begin) ctl->list_fallbacks += 1;
     if (done) {
         if (!converged) ctl->status |= 1u;
         ctl->status_all |= ctl->status;
@@ -289,7 +290,7 @@ __device__ __forceinline__ float pressure_body(const PS& ps, const ListBuffers& 
         const DevParams& P = ps.params(i);
         Control* ctl = ps.control(i);
         // no particle of the scene moved more than half the skin: its lists are complete for x*
-        const bool all_lists_ok = ctl->any_fast == 0u;
+        const bool all_lists_ok = ctl->fast_particles == ctl->fast_at_begin;
         const float4 xi = b.pos[i];
         const float4 xp = b.pred[i];
         float acc = 0.f;
@@ -537,7 +538,7 @@ __global__ void k_batch_begin(DevParams* table, Control* ctls, uint32_t n_scenes
         c->done = 0;
         c->finished = 0;
         c->max_err_bits = 0;
-        c->any_fast = 0;
+        c->fast_at_begin = c->fast_particles;
         c->status = 0;
     }
     if (threadIdx.x == 0) {

@@ -93,7 +93,7 @@ __global__ void k_begin(Control* ctl) {
     ctl->status = 0;
     ctl->guard_iters = 0;
     ctl->n_groups = 0;
-    ctl->any_fast = 0;
+    ctl->fast_at_begin = ctl->fast_particles;
 }
 
 // pcisph.cl:65-92
