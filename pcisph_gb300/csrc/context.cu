@@ -94,6 +94,7 @@ struct pcisph_ctx {
     DevParams P{};
     SweepGrid sweep_grid{};
     size_t list_n = 0;
+    bool list_bnd = false;  // the list block holds the boundary lists
 
     SweepArgs sweep_args() const {
         return SweepArgs{b.groups, &b.ctl->n_groups, sorted_keys, b.cells, b.b_cells, b.codes, b.b_codes};
@@ -110,7 +111,7 @@ struct pcisph_ctx {
         return ListBuffers{b.pos, b.vel, b.pr4, b.normal, b.f_other, b.f_press, b.pred, b.pf4, b.state_pos,
                            b.state_vel, b.rho, b.press, b.err, w ? cells_w : b.cells, b.b_cells, b.b_pos, b.bpf,
                            b.nbr, b.nbr_count, b.near, b.near_count, b.bucket_fast, P.fluid_count,
-                           w ? d_of_w : nullptr, b.b_init, b.b_press, b.b_near};
+                           w ? d_of_w : nullptr, b.b_init, b.b_press, b.b_near, b.bnbr, b.bnbr_count};
     }
 
     // Working-order buffers for n particles and bk buckets; the index maps start as the identity.
@@ -194,9 +195,11 @@ struct pcisph_ctx {
         if (!list_sweeps()) return PCISPH_OK;
         const size_t n = params.fluid_count;
         if (n >= (1u << 31)) return fail(PCISPH_ERR_INVALID_ARG, "kernel variant 2 takes fewer than 2^31 particles");
+        const bool bnd = params.boundary_count > 0;
         const size_t bytes = align256(n * P.list_cap * 4) + align256(n * 4) + align256(n * P.near_cap * 4) +
-                             align256(n * 4) + align256(params.bucket_count) + align256(n);
-        if (list_block.p && list_block.cap >= bytes && list_n == n) return PCISPH_OK;
+                             align256(n * 4) + align256(params.bucket_count) + align256(n) +
+                             (bnd ? align256(n * P.bnd_cap * 4) + align256(n * 4) : 0);
+        if (list_block.p && list_block.cap >= bytes && list_n == n && list_bnd == bnd) return PCISPH_OK;
         CUDA_TRY(cudaStreamSynchronize(stream()));
         if (list_block.ensure(bytes) != cudaSuccess)
             return fail(PCISPH_ERR_OOM, "device allocation of the neighbour lists failed");
@@ -207,7 +210,10 @@ struct pcisph_ctx {
         b.near_count = c.take<uint32_t>(n);
         b.bucket_fast = c.take<unsigned char>(params.bucket_count);
         b.b_near = c.take<unsigned char>(n);
+        b.bnbr = bnd ? c.take<uint32_t>(n * P.bnd_cap) : nullptr;
+        b.bnbr_count = bnd ? c.take<uint32_t>(n) : nullptr;
         list_n = n;
+        list_bnd = bnd;
         graph_valid = false;
         order_age = kNoOrder;
         return PCISPH_OK;

@@ -189,8 +189,9 @@ __device__ __forceinline__ void decide(const DevParams& P, Control* ctl) {
     }
 }
 
-// pcisph.cl:65-92, and the neighbour list of the step
-template <class PS>
+// pcisph.cl:65-92, and the neighbour list of the step. kBoundary: the scene has boundary particles (their
+// walk and list are compiled out otherwise: the fluid-only builder measured 5% slower with them present)
+template <class PS, bool kBoundary>
 __global__ void __launch_bounds__(kBlock) k_density_list(PS ps, ListBuffers b) {
     const uint32_t i = blockIdx.x * kBlock + threadIdx.x;
     if (i >= ps.count()) return;
@@ -198,21 +199,33 @@ __global__ void __launch_bounds__(kBlock) k_density_list(PS ps, ListBuffers b) {
     const float4 xi = b.pos[i];
     const Cell c = cell_of(xi.x, xi.y, xi.z, P);
     float acc = 0.f;
-    if (P.boundary_count) {
-        bool near_b = false;  // some boundary particle within r_list: the later sweeps must walk the boundary
+    const uint32_t stride = b.nbr_stride;
+    // current chunk of each thread's skin and within-h lists; the boundary list's chunks go through the
+    // within-h buffer before the fluid walk starts (more shared memory would take it from the L1 cache)
+    __shared__ uint32_t staged[2][8 * kBlock];
+    uint32_t* fbuf = staged[0];
+    uint32_t* nbuf = staged[1];
+    if (kBoundary && P.boundary_count) {
+        // boundary particles within r_list, in walk order: the later sweeps read them from the boundary list
+        // (all of them, or walk the boundary buckets when there are more than bnd_cap)
+        uint32_t nb = 0;
+        uint32_t* bbuf = staged[1];
         for_each_neighbour(b.b_cells, c, P, [&](uint32_t j) {
             const float4 o = __ldg(&b.b_pos[j]);
             const float r2 = dist2(xi.x - o.x, xi.y - o.y, xi.z - o.z);
             acc += poly6(r2, P.h2);  // density_term's expression
-            near_b |= r2 <= P.list_r2;
+            if (r2 <= P.list_r2) {
+                if (b.bnbr && nb < P.bnd_cap) list_append(b.bnbr, i, stride, bbuf, nb, j);
+                ++nb;
+            }
         });
-        b.b_near[i] = near_b ? 1 : 0;
+        b.b_near[i] = nb ? 1 : 0;
+        if (b.bnbr) {
+            list_finish(b.bnbr, i, stride, bbuf, nb, P.bnd_cap);
+            b.bnbr_count[i] = nb;
+        }
     }
-    const uint32_t stride = b.nbr_stride;
     uint32_t n = 0, nn = 0;
-    __shared__ uint32_t staged[2][8 * kBlock];  // current chunk of each thread's skin and within-h lists
-    uint32_t* fbuf = staged[0];
-    uint32_t* nbuf = staged[1];
     auto load = [&](uint32_t j) { return __ldg(&b.pos[j]); };
     auto use = [&](uint32_t j, const float4& o) {
         const float dx = xi.x - o.x, dy = xi.y - o.y, dz = xi.z - o.z;
@@ -297,17 +310,26 @@ __device__ __forceinline__ float pressure_body(const PS& ps, const ListBuffers& 
         const uint32_t cnt = b.nbr_count[i];
         const bool overflow = cnt > P.list_cap;
         // boundary terms: all zero unless a boundary particle was within r_list of x, or x* moved more than
-        // half the skin from x (boundary particles do not move)
-        bool walk_boundary = false;
+        // half the skin from x (boundary particles do not move). Within half the skin, the boundary list
+        // (every boundary particle within r_list of x) holds every one that can be within h of x*.
+        bool walk_boundary = false, list_boundary = false;
+        uint32_t bcnt = 0;
         if (P.boundary_count) {
             const float dx = xp.x - xi.x, dy = xp.y - xi.y, dz = xp.z - xi.z;
-            walk_boundary = b.b_near[i] != 0 || sqrtf(dist2(dx, dy, dz)) > P.list_half_skin;
+            if (sqrtf(dist2(dx, dy, dz)) > P.list_half_skin) {
+                walk_boundary = true;
+            } else if (b.b_near[i] != 0) {
+                if (b.bnbr) bcnt = b.bnbr_count[i];
+                list_boundary = b.bnbr && bcnt <= P.bnd_cap;
+                walk_boundary = !list_boundary;
+            }
         }
         Cell c{0u, 0u, 0u};  // the cell (three IEEE divisions) only where a walk may need it
         if (overflow || !all_lists_ok || walk_boundary) c = cell_of(xi.x, xi.y, xi.z, P);
         const bool walk = overflow || (!all_lists_ok && near_fast(P, b.bucket_fast, c));
-        if (walk_boundary)
-            for_each_neighbour(b.b_cells, c, P, [&](uint32_t j) { acc += density_term(xp.x, xp.y, xp.z, __ldg(&b.b_pos[j]), P.h2); });
+        auto fb = [&](uint32_t j) { acc += density_term(xp.x, xp.y, xp.z, __ldg(&b.b_pos[j]), P.h2); };
+        if (walk_boundary) for_each_neighbour(b.b_cells, c, P, fb);
+        else if (list_boundary) for_each_listed(b.bnbr, i, bcnt, b.nbr_stride, fb);
         auto f = [&](uint32_t j) { acc += density_term(xp.x, xp.y, xp.z, __ldg(&b.pred[j]), P.h2); };
         if (walk) for_each_neighbour(b.cells, c, P, f);
         else for_each_listed(b.nbr, i, cnt, b.nbr_stride, f);
@@ -367,12 +389,17 @@ __device__ __forceinline__ void pressure_force_body(const PS& ps, const ListBuff
     const float4 xi = b.pf4[i];
     float3 f = make_float3(0.f, 0.f, 0.f);
     const uint32_t cnt = b.near_count[i];
-    // boundary terms at x (within h): all zero unless a boundary particle was within r_list of x
-    const bool walk_boundary = P.boundary_count && b.b_near[i] != 0;
+    // boundary terms at x (within h): all zero unless a boundary particle was within r_list of x; the
+    // boundary list holds every one within r_list (terms beyond h are zero)
+    const bool near_b = P.boundary_count && b.b_near[i] != 0;
+    const uint32_t bcnt = near_b && b.bnbr ? b.bnbr_count[i] : 0u;
+    const bool list_boundary = near_b && b.bnbr && bcnt <= P.bnd_cap;
+    const bool walk_boundary = near_b && !list_boundary;
     Cell c{0u, 0u, 0u};
     if (cnt > P.near_cap || walk_boundary) c = cell_of(xi.x, xi.y, xi.z, P);
-    if (walk_boundary)
-        for_each_neighbour(b.b_cells, c, P, [&](uint32_t j) { pressure_force_term(xi, __ldg(&b.bpf[j]), P.h, P.h2, f); });
+    auto fb = [&](uint32_t j) { pressure_force_term(xi, __ldg(&b.bpf[j]), P.h, P.h2, f); };
+    if (walk_boundary) for_each_neighbour(b.b_cells, c, P, fb);
+    else if (list_boundary) for_each_listed(b.bnbr, i, bcnt, b.nbr_stride, fb);
     auto body = [&](uint32_t j) { pressure_force_term(xi, __ldg(&b.pf4[j]), P.h, P.h2, f); };
     if (cnt <= P.near_cap) for_each_listed(b.near, i, cnt, b.nbr_stride, body);
     else for_each_neighbour(b.cells, c, P, body);
@@ -411,7 +438,8 @@ __device__ __forceinline__ void pressure_force_body(const PS& ps, const ListBuff
 }
 
 template <class PS, int BS = kBlock>
-__global__ void __launch_bounds__(BS) k_pressure_force_list(PS ps, ListBuffers b, int mode,
+// (at most 40 registers: 48 resident warps per SM; 48 registers measured 10% slower at 1M)
+__global__ void __launch_bounds__(BS, 1536 / BS) k_pressure_force_list(PS ps, ListBuffers b, int mode,
                                                             cudaGraphConditionalHandle cond, int use_cond) {
     const uint32_t i = blockIdx.x * BS + threadIdx.x;
     if (!PS::kBatched && use_cond && i == 0) {
@@ -575,7 +603,8 @@ __global__ void __launch_bounds__(kBlock) k_hash_scenes(SceneTable ps, const flo
 }  // namespace
 
 void launch_density_list(const DevParams& P, Control* ctl, const ListBuffers& b, cudaStream_t s) {
-    k_density_list<<<grid_for(P.fluid_count), kBlock, 0, s>>>(OneScene{P, ctl}, b);
+    if (P.boundary_count) k_density_list<OneScene, true><<<grid_for(P.fluid_count), kBlock, 0, s>>>(OneScene{P, ctl}, b);
+    else k_density_list<OneScene, false><<<grid_for(P.fluid_count), kBlock, 0, s>>>(OneScene{P, ctl}, b);
 }
 void launch_normal_list(const DevParams& P, Control* ctl, const ListBuffers& b, cudaStream_t s) {
     k_normal_list<<<grid_for(P.fluid_count), kBlock, 0, s>>>(OneScene{P, ctl}, b);
@@ -643,7 +672,7 @@ void launch_hash_scenes(const SceneTable& t, const float4* pos, uint32_t* keys, 
     if (t.n) k_hash_scenes<<<grid_for(t.n), kBlock, 0, s>>>(t, pos, keys);
 }
 void launch_density_scenes(const SceneTable& t, const ListBuffers& b, cudaStream_t s) {
-    if (t.n) k_density_list<<<grid_for(t.n), kBlock, 0, s>>>(t, b);
+    if (t.n) k_density_list<SceneTable, false><<<grid_for(t.n), kBlock, 0, s>>>(t, b);  // no boundary in a batch
 }
 void launch_normal_scenes(const SceneTable& t, const ListBuffers& b, cudaStream_t s) {
     if (t.n) k_normal_list<<<grid_for(t.n), kBlock, 0, s>>>(t, b);

@@ -27,6 +27,9 @@ struct ListBuffers {
     float* b_press;
     unsigned char* b_near;       // per fluid particle (B > 0): a boundary particle within r_list of x at the
                                  // step's start; 0: the boundary terms of the step's sweeps are all zero
+    uint32_t* bnbr;              // per fluid particle (B > 0, or null): the boundary particles within r_list
+                                 // of x in walk order, bnd_cap entries laid out like nbr
+    uint32_t* bnbr_count;        // entries per particle; > bnd_cap: walk the boundary buckets
 };
 
 // One scene: parameters by value; the pressure kernel's last block decides the loop.

@@ -30,6 +30,8 @@ struct StepBuffers {
     uint32_t* near_count;            // entries per particle; > near_cap means "walk the buckets"
     unsigned char* bucket_fast;      // per bucket: holds a particle predicted to move > skin / 2 (this step)
     unsigned char* b_near;           // per particle (B > 0): a boundary particle within the list radius
+    uint32_t* bnbr;                  // per particle (B > 0): boundary particles within the list radius
+    uint32_t* bnbr_count;            // entries per particle; > bnd_cap means "walk the boundary buckets"
     // boundary
     float4 *b_pos, *bpf;
     float *b_press, *b_init;

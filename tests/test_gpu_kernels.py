@@ -646,6 +646,35 @@ def test_boundary_scene_step_error_vs_fp64(oracle, variant):
         assert e_gpu <= 10 * e_cpu + 1e-6, (name, e_gpu, e_cpu)
 
 
+@pytest.mark.parametrize("loop_mode", [0, 2])
+def test_boundary_lists_change_no_bits(oracle, loop_mode):
+    """Near-wall particles read their boundary neighbours from the boundary list (every boundary particle
+    within r_list of x, in walk order) instead of walking the boundary buckets: the same terms in the same
+    order. Skin 0 makes every prediction outrun its lists, so every sweep walks; skins 0, 0.25 and 0.5 give
+    the same bits (fluid block in a boundary box, some particles thrown at the walls)."""
+    d = 0.02
+    pos = scenes.lattice_block(10, 12, 10, d, (2 * d, 0.0, 2 * d), seed=19)
+    b_pos = scenes.boundary_box((0.0, 0.0, 0.0), (14 * d, 20 * d, 14 * d), d, layers=2)
+    rng = np.random.default_rng(19)
+    vel = (rng.standard_normal(pos.shape) * 0.05).astype(np.float32)
+    fast = rng.choice(pos.shape[0], 40, replace=False)
+    vel[fast] = (rng.standard_normal((40, 3)) * 4.0).astype(np.float32)
+    p = oracle.derive_params(0.5 * d, 1000.0, pos.shape[0], b_pos.shape[0], 1e-3, -9.81, 0.2 * d ** 3, 0.5)
+    out = {}
+    for skin in (0.0, 0.25, 0.5):
+        f = fluid_like(p, min_iters=4, max_iters=4, kernel_variant=2, loop_mode=loop_mode)
+        f.set_options(list_skin=skin)
+        f.set_fluid_state(pos, vel)
+        f.set_boundary_state(b_pos)
+        f.step(3)
+        out[skin] = {n: f.get_field(n) for n in ("position", "velocity", "density", "pressure", "pressure_force",
+                                                 "boundary_pressure")}
+        f.close()
+    for skin in (0.25, 0.5):
+        for n, w in out[0.0].items():
+            np.testing.assert_array_equal(out[skin][n], w, err_msg=f"skin {skin}: {n}")
+
+
 def test_rederive_after_autotune_keeps_a_valid_sort_scratch():
     """Parameters changed after autotuning re-derive the scene (and the default sort digit width): the next
     steps still sort, with a scratch sized for that width."""
