@@ -29,6 +29,7 @@ struct DevParams {
     uint32_t list_cap;
     uint32_t near_cap;  // entries of the within-h list
     uint32_t bnd_cap;   // entries of the boundary list (boundary particles within r_list)
+    uint32_t bfl_cap;   // entries of a boundary particle's fluid list (fluid particles within r_list)
     float near_r2;      // within-h list radius^2: h^2 (1 + 1e-4), a margin far above rounding
     float list_r, list_r2, list_half_skin;
     // batched scenes with an adaptive skin: each step picks one of kSkinLevels skins from the previous

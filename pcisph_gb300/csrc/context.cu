@@ -94,7 +94,7 @@ struct pcisph_ctx {
     DevParams P{};
     SweepGrid sweep_grid{};
     size_t list_n = 0;
-    bool list_bnd = false;  // the list block holds the boundary lists
+    size_t list_b_n = 0;  // boundary particles the list block holds lists for
 
     SweepArgs sweep_args() const {
         return SweepArgs{b.groups, &b.ctl->n_groups, sorted_keys, b.cells, b.b_cells, b.codes, b.b_codes};
@@ -111,7 +111,8 @@ struct pcisph_ctx {
         return ListBuffers{b.pos, b.vel, b.pr4, b.normal, b.f_other, b.f_press, b.pred, b.pf4, b.state_pos,
                            b.state_vel, b.rho, b.press, b.err, w ? cells_w : b.cells, b.b_cells, b.b_pos, b.bpf,
                            b.nbr, b.nbr_count, b.near, b.near_count, b.bucket_fast, P.fluid_count,
-                           w ? d_of_w : nullptr, b.b_init, b.b_press, b.b_near, b.bnbr, b.bnbr_count};
+                           w ? d_of_w : nullptr, b.b_init, b.b_press, b.b_near, b.bnbr, b.bnbr_count, b.bfl,
+                           b.bfl_count};
     }
 
     // Working-order buffers for n particles and bk buckets; the index maps start as the identity.
@@ -195,11 +196,14 @@ struct pcisph_ctx {
         if (!list_sweeps()) return PCISPH_OK;
         const size_t n = params.fluid_count;
         if (n >= (1u << 31)) return fail(PCISPH_ERR_INVALID_ARG, "kernel variant 2 takes fewer than 2^31 particles");
-        const bool bnd = params.boundary_count > 0;
+        const size_t nb = params.boundary_count;
+        const bool bnd = nb > 0;
         const size_t bytes = align256(n * P.list_cap * 4) + align256(n * 4) + align256(n * P.near_cap * 4) +
                              align256(n * 4) + align256(params.bucket_count) + align256(n) +
-                             (bnd ? align256(n * P.bnd_cap * 4) + align256(n * 4) : 0);
-        if (list_block.p && list_block.cap >= bytes && list_n == n && list_bnd == bnd) return PCISPH_OK;
+                             (bnd ? align256(n * P.bnd_cap * 4) + align256(n * 4) + align256(nb * P.bfl_cap * 4) +
+                                        align256(nb * 4)
+                                  : 0);
+        if (list_block.p && list_block.cap >= bytes && list_n == n && list_b_n == nb) return PCISPH_OK;
         CUDA_TRY(cudaStreamSynchronize(stream()));
         if (list_block.ensure(bytes) != cudaSuccess)
             return fail(PCISPH_ERR_OOM, "device allocation of the neighbour lists failed");
@@ -212,8 +216,10 @@ struct pcisph_ctx {
         b.b_near = c.take<unsigned char>(n);
         b.bnbr = bnd ? c.take<uint32_t>(n * P.bnd_cap) : nullptr;
         b.bnbr_count = bnd ? c.take<uint32_t>(n) : nullptr;
+        b.bfl = bnd ? c.take<uint32_t>(nb * P.bfl_cap) : nullptr;
+        b.bfl_count = bnd ? c.take<uint32_t>(nb) : nullptr;
         list_n = n;
-        list_bnd = bnd;
+        list_b_n = nb;
         graph_valid = false;
         order_age = kNoOrder;
         return PCISPH_OK;
@@ -416,6 +422,10 @@ struct pcisph_ctx {
         if (list_sweeps()) {
             timed("density", s, [&] { launch_density_list(P, b.ctl, list_buffers(), s); });
             timed("normal", s, [&] { launch_normal_list(P, b.ctl, list_buffers(), s); });
+            if (B) {
+                timed("boundary_list", s, [&] { launch_boundary_fluid_list(P, list_buffers(), s); });
+                ++nl;
+            }
         } else if (warp_sweeps()) {
             timed("density", s, [&] { launch_density_sweep(P, b, A, sweep_grid, s); });
             timed("normal", s, [&] { launch_normal_sweep(P, b, A, sweep_grid, s); });
@@ -435,7 +445,10 @@ struct pcisph_ctx {
     int record_iteration(cudaStream_t s, cudaGraphConditionalHandle cond, bool use_cond) {
         int nl = 0;
         if (params.boundary_count) {
-            timed("boundary_pressure", s, [&] { launch_boundary_pressure(P, b, working_order() ? cells_w : b.cells, s); });
+            if (list_sweeps())
+                timed("boundary_pressure", s, [&] { launch_boundary_pressure_list(P, b.ctl, list_buffers(), s); });
+            else
+                timed("boundary_pressure", s, [&] { launch_boundary_pressure(P, b, working_order() ? cells_w : b.cells, s); });
             ++nl;
         }
         if (list_sweeps()) {

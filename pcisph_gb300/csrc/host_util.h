@@ -27,6 +27,7 @@ inline constexpr float kPi = 3.14159265358979323846f;  // utils/constants.h:4
 inline constexpr uint32_t kListCap = 96;           // neighbour-list entries per particle (multiple of 4)
 inline constexpr uint32_t kNearCap = 64;           // within-h list entries per particle
 inline constexpr uint32_t kBoundaryListCap = 48;   // boundary particles within r_list per fluid particle
+inline constexpr uint32_t kBoundaryFluidCap = 64;  // fluid particles within r_list per boundary particle
 // skin-list entries per particle of a batch (skins up to 0.5 h: ~48 (1 + skin)^3 entries at rest density)
 inline constexpr uint32_t kListCapWide = 168;
 // adaptive skin: a level qualifies if at most 1 in this many of the last step's predictions outran it
@@ -272,6 +273,7 @@ inline void make_devparams(const pcisph_sim_params& p, int min_iters, int max_it
     d->list_cap = list_cap;
     d->near_cap = kNearCap;
     d->bnd_cap = kBoundaryListCap;
+    d->bfl_cap = kBoundaryFluidCap;
     d->near_r2 = p.kernel_radius2 * 1.0001f;
     set_list_skin(d, list_skin);
     d->adaptive_skin = adaptive_skin;

@@ -167,6 +167,52 @@ __device__ __forceinline__ bool near_fast(const DevParams& P, const unsigned cha
     return any;
 }
 
+// The fluid particles within r_list of boundary particle k at the step's start, in the order of the walk
+// of pcisph.cl:212-263 with boundary_update = 1 (27 fluid buckets around the boundary particle's cell).
+__global__ void __launch_bounds__(kBlock) k_boundary_fluid_list(DevParams P, ListBuffers b) {
+    const uint32_t k = blockIdx.x * kBlock + threadIdx.x;
+    if (k >= P.boundary_count) return;
+    const float4 xb = b.b_pos[k];
+    const Cell c = cell_of(xb.x, xb.y, xb.z, P);
+    __shared__ uint32_t staged[8 * kBlock];
+    const uint32_t stride = P.boundary_count;
+    uint32_t n = 0;
+    for_each_neighbour(b.cells, c, P, [&](uint32_t j) {
+        const float4 o = __ldg(&b.pos[j]);
+        if (dist2(xb.x - o.x, xb.y - o.y, xb.z - o.z) <= P.list_r2) {
+            if (n < P.bfl_cap) list_append(b.bfl, k, stride, staged, n, j);
+            ++n;
+        }
+    });
+    list_finish(b.bfl, k, stride, staged, n, P.bfl_cap);
+    b.bfl_count[k] = n;
+}
+
+// pcisph.cl:212-263 with boundary_update = 1 from boundary particle k's fluid list: a fluid particle not
+// listed was farther than r_list from x_b at the step's start, so it is farther than h from x_b at its
+// prediction unless it moved more than half the skin, which flags its bucket (then k walks).
+__device__ __forceinline__ void boundary_pressure_list_body(const DevParams& P, const Control* ctl,
+                                                            const ListBuffers& b, uint32_t k) {
+    if (k >= P.boundary_count) return;
+    const float4 xb = b.b_pos[k];
+    float acc = b.b_init[k];
+    const uint32_t cnt = b.bfl_count[k];
+    bool walk = cnt > P.bfl_cap;
+    Cell c{0u, 0u, 0u};
+    if (walk || ctl->fast_particles != ctl->fast_at_begin) {
+        c = cell_of(xb.x, xb.y, xb.z, P);
+        walk = walk || near_fast(P, b.bucket_fast, c);
+    }
+    auto f = [&](uint32_t j) { boundary_density_term(xb, __ldg(&b.pred[j]), P.h2, acc); };
+    if (walk) for_each_neighbour(b.cells, c, P, f);
+    else for_each_listed(b.bfl, k, cnt, P.boundary_count, f);
+    boundary_pressure_finish(P, xb, acc, b.b_press, const_cast<float4*>(b.bpf), k);
+}
+
+__global__ void __launch_bounds__(kBlock) k_boundary_pressure_list(DevParams P, const Control* ctl, ListBuffers b) {
+    boundary_pressure_list_body(P, ctl, b, blockIdx.x * kBlock + threadIdx.x);
+}
+
 // The loop decision of one scene after its pressure sweep (Fluid.cpp:284-306).
 __device__ __forceinline__ void decide(const DevParams& P, Control* ctl) {
     const float mx = __uint_as_float(ctl->max_err_bits);
@@ -468,7 +514,7 @@ __global__ void __launch_bounds__(kBlock) k_corrective_loop(PS ps, ListBuffers b
         if constexpr (!PS::kBatched) {  // boundary pressures at the predicted positions (read by the force)
             const DevParams& P = ps.params(0);
             for (uint32_t k = blockIdx.x * kBlock + threadIdx.x; k < P.boundary_count; k += stride)
-                boundary_pressure_body(P, b.cells, b.pred, b.b_pos, b.b_init, b.b_press, const_cast<float4*>(b.bpf), k);
+                boundary_pressure_list_body(P, ps.control(0), b, k);
         }
         unsigned local = 0;
         for (uint32_t r = 0; r < rounds; ++r)
@@ -662,6 +708,12 @@ cudaError_t launch_corrective_loop_scenes(const SceneTable& t, const ListBuffers
     return launch_loop(t, t.n, b, batch, max_iters, s);
 }
 
+void launch_boundary_fluid_list(const DevParams& P, const ListBuffers& b, cudaStream_t s) {
+    if (P.boundary_count) k_boundary_fluid_list<<<grid_for(P.boundary_count), kBlock, 0, s>>>(P, b);
+}
+void launch_boundary_pressure_list(const DevParams& P, Control* ctl, const ListBuffers& b, cudaStream_t s) {
+    if (P.boundary_count) k_boundary_pressure_list<<<grid_for(P.boundary_count), kBlock, 0, s>>>(P, ctl, b);
+}
 void launch_batch_begin(DevParams* table, Control* ctls, uint32_t n_scenes, Control* batch, cudaStream_t s) {
     k_batch_begin<<<1, 256, 0, s>>>(table, ctls, n_scenes, batch);
 }

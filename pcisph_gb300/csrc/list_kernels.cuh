@@ -30,6 +30,10 @@ struct ListBuffers {
     uint32_t* bnbr;              // per fluid particle (B > 0, or null): the boundary particles within r_list
                                  // of x in walk order, bnd_cap entries laid out like nbr
     uint32_t* bnbr_count;        // entries per particle; > bnd_cap: walk the boundary buckets
+    uint32_t* bfl;               // per boundary particle (B > 0, or null): the fluid particles within r_list
+                                 // of it at the step's start, walk order, bfl_cap entries chunked over the
+                                 // boundary particles (stride boundary_count)
+    uint32_t* bfl_count;         // entries per boundary particle; > bfl_cap: walk the fluid buckets
 };
 
 // One scene: parameters by value; the pressure kernel's last block decides the loop.
@@ -62,6 +66,11 @@ struct SceneTable {
 };
 
 void launch_density_list(const DevParams& P, Control* ctl, const ListBuffers& b, cudaStream_t s);
+// Boundary particles (B > 0): their fluid lists at the step's start, and their pressure update per
+// iteration from those lists (walking the fluid buckets when a fast fluid particle is near or a list
+// overflowed). One scene.
+void launch_boundary_fluid_list(const DevParams& P, const ListBuffers& b, cudaStream_t s);
+void launch_boundary_pressure_list(const DevParams& P, Control* ctl, const ListBuffers& b, cudaStream_t s);
 void launch_normal_list(const DevParams& P, Control* ctl, const ListBuffers& b, cudaStream_t s);
 void launch_force_list(const DevParams& P, Control* ctl, const ListBuffers& b, cudaStream_t s);
 // block: threads per block of the two corrective-loop sweeps (128, 256 or 512)

@@ -75,6 +75,29 @@ __device__ __forceinline__ void pressure_force_term(const float4& xi, const floa
     }
 }
 
+// One fluid particle's term in a boundary particle's predicted density (pcisph.cl:240-250 from the boundary
+// side: distance from x_b to the fluid particle's predicted position)
+__device__ __forceinline__ void boundary_density_term(const float4& xb, const float4& o, float h2, float& acc) {
+    const float dx = xb.x - o.x, dy = xb.y - o.y, dz = xb.z - o.z;
+    acc += poly6(dist2(dx, dy, dz), h2);
+}
+
+// The rest of a boundary particle's pressure update from its density sum acc (self density included):
+// pressure increment delta * max(0, rho* - rho0) and the packed operand (x_b, p_b / rho0^2).
+__device__ __forceinline__ void boundary_pressure_finish(const DevParams& P, const float4& xb, float acc,
+                                                         float* __restrict__ b_press, float4* __restrict__ bpf,
+                                                         uint32_t i) {
+    acc *= P.particle_mass * P.poly6_norm;
+    float dv = acc - P.rest_density;
+    dv = 0.f < dv ? dv : 0.f;
+    float p = b_press[i];
+    if (dv != 0.f) {
+        p += dv * P.delta;
+        b_press[i] = p;
+    }
+    bpf[i] = make_float4(xb.x, xb.y, xb.z, p / (P.rest_density * P.rest_density));
+}
+
 // One boundary particle's pressure update at the predicted fluid positions (pcisph.cl:212-263 with
 // boundary_update = 1): predicted density from its initial (self) density plus the fluid neighbours,
 // pressure increment delta * max(0, rho* - rho0), and its packed operand (x_b, p_b / rho0^2) for the
@@ -88,20 +111,8 @@ __device__ __forceinline__ void boundary_pressure_body(const DevParams& P, const
     const float4 xb = b_pos[i];
     const Cell c = cell_of(xb.x, xb.y, xb.z, P);
     float acc = b_init[i];
-    for_each_neighbour(cells, c, P, [&](uint32_t j) {
-        const float4 o = __ldg(&pred[j]);
-        const float dx = xb.x - o.x, dy = xb.y - o.y, dz = xb.z - o.z;
-        acc += poly6(dist2(dx, dy, dz), P.h2);
-    });
-    acc *= P.particle_mass * P.poly6_norm;
-    float dv = acc - P.rest_density;
-    dv = 0.f < dv ? dv : 0.f;
-    float p = b_press[i];
-    if (dv != 0.f) {
-        p += dv * P.delta;
-        b_press[i] = p;
-    }
-    bpf[i] = make_float4(xb.x, xb.y, xb.z, p / (P.rest_density * P.rest_density));
+    for_each_neighbour(cells, c, P, [&](uint32_t j) { boundary_density_term(xb, __ldg(&pred[j]), P.h2, acc); });
+    boundary_pressure_finish(P, xb, acc, b_press, bpf, i);
 }
 
 }  // namespace pcisph

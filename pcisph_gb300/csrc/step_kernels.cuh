@@ -32,6 +32,8 @@ struct StepBuffers {
     unsigned char* b_near;           // per particle (B > 0): a boundary particle within the list radius
     uint32_t* bnbr;                  // per particle (B > 0): boundary particles within the list radius
     uint32_t* bnbr_count;            // entries per particle; > bnd_cap means "walk the boundary buckets"
+    uint32_t* bfl;                   // per boundary particle: fluid particles within the list radius
+    uint32_t* bfl_count;             // entries per boundary particle; > bfl_cap means "walk"
     // boundary
     float4 *b_pos, *bpf;
     float *b_press, *b_init;
