@@ -646,15 +646,19 @@ def test_boundary_scene_step_error_vs_fp64(oracle, variant):
         assert e_gpu <= 10 * e_cpu + 1e-6, (name, e_gpu, e_cpu)
 
 
-@pytest.mark.parametrize("loop_mode", [0, 2])
-def test_boundary_lists_change_no_bits(oracle, loop_mode):
+@pytest.mark.parametrize("loop_mode,b_spacing,f_spacing", [(0, 1.0, 1.0), (2, 1.0, 1.0), (0, 0.5, 1.0), (0, 1.0, 0.7)])
+def test_boundary_lists_change_no_bits(oracle, loop_mode, b_spacing, f_spacing):
     """Near-wall particles read their boundary neighbours from the boundary list (every boundary particle
-    within r_list of x, in walk order) instead of walking the boundary buckets: the same terms in the same
-    order. Skin 0 makes every prediction outrun its lists, so every sweep walks; skins 0, 0.25 and 0.5 give
-    the same bits (fluid block in a boundary box, some particles thrown at the walls)."""
+    within r_list of x, in walk order) and boundary particles their fluid neighbours from theirs, instead of
+    walking the buckets: the same terms in the same order. Skin 0 makes every prediction outrun its lists,
+    so every sweep walks; skins 0, 0.25 and 0.5 give the same bits (fluid block in a boundary box, some
+    particles thrown at the walls). Boundary particles at half the fluid spacing, four layers deep,
+    overflow the 48-entry boundary lists of the near-wall particles; fluid at 0.7 of its spacing overflows
+    the 64-entry fluid lists of the boundary particles (and the fluid's own lists): those walk."""
     d = 0.02
-    pos = scenes.lattice_block(10, 12, 10, d, (2 * d, 0.0, 2 * d), seed=19)
-    b_pos = scenes.boundary_box((0.0, 0.0, 0.0), (14 * d, 20 * d, 14 * d), d, layers=2)
+    pos = scenes.lattice_block(10, 12, 10, d * f_spacing, (2 * d, 0.0, 2 * d), seed=19)
+    db = d * b_spacing
+    b_pos = scenes.boundary_box((0.0, 0.0, 0.0), (14 * d, 20 * d, 14 * d), db, layers=2 if b_spacing == 1.0 else 4)
     rng = np.random.default_rng(19)
     vel = (rng.standard_normal(pos.shape) * 0.05).astype(np.float32)
     fast = rng.choice(pos.shape[0], 40, replace=False)
