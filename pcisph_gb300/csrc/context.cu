@@ -16,6 +16,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -74,6 +75,13 @@ struct pcisph_ctx {
 
     DeviceBlock fluid_block, boundary_block, misc_block, sort_block, staging_block, list_block, order_block,
         bucket_sort_block;
+    // the boundary zone (list sweeps, B > 0): cell bounds scratch, then one byte per cell of the boundary's
+    // cell box widened by two; zone_map null when the box has more than kZoneMaxCells cells
+    static constexpr uint64_t kZoneMaxCells = 1ull << 26;
+    DeviceBlock zone_block;
+    unsigned char* zone_map = nullptr;
+    int zone_org[3] = {0, 0, 0};
+    uint32_t zone_dim[3] = {0, 0, 0};
     // working order (variant 2 with spatial_order): bucket ranges in working order, bucket Morton codes,
     // the two index maps, scan scratch, and a transfer buffer for fields exported or imported in sorted order
     uint2* cells_w = nullptr;
@@ -112,7 +120,8 @@ struct pcisph_ctx {
                            b.state_vel, b.rho, b.press, b.err, w ? cells_w : b.cells, b.b_cells, b.b_pos, b.bpf,
                            b.nbr, b.nbr_count, b.near, b.near_count, b.bucket_fast, P.fluid_count,
                            w ? d_of_w : nullptr, b.b_init, b.b_press, b.b_near, b.bnbr, b.bnbr_count, b.bfl,
-                           b.bfl_count};
+                           b.bfl_count, zone_map, {zone_org[0], zone_org[1], zone_org[2]},
+                           {zone_dim[0], zone_dim[1], zone_dim[2]}};
     }
 
     // Working-order buffers for n particles and bk buckets; the index maps start as the identity.
@@ -392,7 +401,48 @@ struct pcisph_ctx {
         else CUDA_TRY(cudaMemsetAsync(b.b_init, 0, (size_t)B * 4, s));
         host_launches += nl + 1 + (opts.boundary_self_density ? 1 : 0);
         CUDA_TRY(cudaGetLastError());
+        int rc = build_boundary_zone(s);
+        if (rc) return rc;
         boundary_updated = false;
+        return PCISPH_OK;
+    }
+
+    // The boundary zone over the sorted boundary positions (list sweeps only; once per boundary change,
+    // synchronising for the cell bounds). Kernel arguments change, so the step graphs are rebuilt.
+    int build_boundary_zone(cudaStream_t s) {
+        zone_map = nullptr;
+        graph_valid = false;
+        const uint32_t B = params.boundary_count;
+        if (!list_sweeps() || B == 0) return PCISPH_OK;
+        if (zone_block.ensure(256) != cudaSuccess) return fail(PCISPH_ERR_OOM, "device allocation of the boundary zone failed");
+        int* bounds = static_cast<int*>(zone_block.p);
+        int h[6] = {INT_MAX, INT_MAX, INT_MAX, INT_MIN, INT_MIN, INT_MIN};
+        CUDA_TRY(cudaMemcpyAsync(bounds, h, sizeof(h), cudaMemcpyHostToDevice, s));
+        launch_boundary_cell_bounds(P, b.b_pos, bounds, s);
+        CUDA_TRY(cudaMemcpyAsync(h, bounds, sizeof(h), cudaMemcpyDeviceToHost, s));
+        CUDA_TRY(cudaStreamSynchronize(s));
+        host_launches += 1;
+        int64_t dim[3];
+        uint64_t cells = 1;
+        for (int a = 0; a < 3; ++a) {
+            if (h[a] < INT_MIN + 2 || h[3 + a] > INT_MAX - 2) return PCISPH_OK;  // saturated cells: no zone
+            dim[a] = (int64_t)h[3 + a] - (int64_t)h[a] + 5;
+            if (dim[a] <= 0 || dim[a] > (int64_t)kZoneMaxCells) return PCISPH_OK;  // no zone: every particle walks
+            cells *= (uint64_t)dim[a];
+            if (cells > kZoneMaxCells) return PCISPH_OK;
+        }
+        if (zone_block.ensure(256 + cells) != cudaSuccess)
+            return fail(PCISPH_ERR_OOM, "device allocation of the boundary zone failed");
+        unsigned char* map = static_cast<unsigned char*>(zone_block.p) + 256;
+        for (int a = 0; a < 3; ++a) {
+            zone_org[a] = (int)((int64_t)h[a] - 2);
+            zone_dim[a] = (uint32_t)dim[a];
+        }
+        CUDA_TRY(cudaMemsetAsync(map, 0, cells, s));
+        launch_boundary_zone(P, b.b_pos, zone_org, zone_dim, map, s);
+        host_launches += 1;
+        CUDA_TRY(cudaGetLastError());
+        zone_map = map;
         return PCISPH_OK;
     }
 
@@ -861,6 +911,7 @@ struct pcisph_ctx {
         sort_block.release();
         staging_block.release();
         list_block.release();
+        zone_block.release();
         order_block.release();
         bucket_sort_block.release();
         for (auto& kv : exports) kv.second.release();

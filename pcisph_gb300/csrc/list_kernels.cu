@@ -188,6 +188,43 @@ __global__ void __launch_bounds__(kBlock) k_boundary_fluid_list(DevParams P, Lis
     b.bfl_count[k] = n;
 }
 
+__global__ void __launch_bounds__(kBlock) k_boundary_cell_bounds(DevParams P, const float4* __restrict__ b_pos,
+                                                                 int* __restrict__ bounds) {
+    const uint32_t k = blockIdx.x * kBlock + threadIdx.x;
+    if (k >= P.boundary_count) return;
+    const float4 xb = b_pos[k];
+    const Cell c = cell_of(xb.x, xb.y, xb.z, P);
+    const int v[3] = {(int)c.x, (int)c.y, (int)c.z};
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const int lo = __reduce_min_sync(__activemask(), v[a]), hi = __reduce_max_sync(__activemask(), v[a]);
+        if ((threadIdx.x & 31) == __ffs(__activemask()) - 1) {
+            atomicMin(&bounds[a], lo);
+            atomicMax(&bounds[3 + a], hi);
+        }
+    }
+}
+
+// Mark every cell within two cells (each axis) of boundary particle k's cell; the box org + [0, dim) holds
+// them all (the boundary's cell bounds widened by two).
+__global__ void __launch_bounds__(kBlock) k_boundary_zone(DevParams P, const float4* __restrict__ b_pos, int ox,
+                                                          int oy, int oz, uint32_t nx, uint32_t ny,
+                                                          unsigned char* __restrict__ zone) {
+    const uint32_t k = blockIdx.x * kBlock + threadIdx.x;
+    if (k >= P.boundary_count) return;
+    const float4 xb = b_pos[k];
+    const Cell c = cell_of(xb.x, xb.y, xb.z, P);
+    const uint32_t x0 = (uint32_t)((int)c.x - ox) - 2u, y0 = (uint32_t)((int)c.y - oy) - 2u,
+                   z0 = (uint32_t)((int)c.z - oz) - 2u;
+#pragma unroll 1
+    for (uint32_t dz = 0; dz < 5; ++dz)
+#pragma unroll 1
+        for (uint32_t dy = 0; dy < 5; ++dy)
+#pragma unroll
+            for (uint32_t dx = 0; dx < 5; ++dx)
+                zone[((size_t)(z0 + dz) * ny + (y0 + dy)) * nx + (x0 + dx)] = 1;
+}
+
 // pcisph.cl:212-263 with boundary_update = 1 from boundary particle k's fluid list: a fluid particle not
 // listed was farther than r_list from x_b at the step's start, so it is farther than h from x_b at its
 // prediction unless it moved more than half the skin, which flags its bucket (then k walks).
@@ -251,7 +288,10 @@ __global__ void __launch_bounds__(kBlock) k_density_list(PS ps, ListBuffers b) {
     __shared__ uint32_t staged[2][8 * kBlock];
     uint32_t* fbuf = staged[0];
     uint32_t* nbuf = staged[1];
-    if (kBoundary && P.boundary_count) {
+    if (kBoundary && P.boundary_count && b.b_zone && !in_boundary_zone(b, c)) {
+        b.b_near[i] = 0;  // every boundary particle is at least 2h away
+        if (b.bnbr) b.bnbr_count[i] = 0;
+    } else if (kBoundary && P.boundary_count) {
         // boundary particles within r_list, in walk order: the later sweeps read them from the boundary list
         // (all of them, or walk the boundary buckets when there are more than bnd_cap)
         uint32_t nb = 0;
@@ -719,6 +759,15 @@ cudaError_t launch_corrective_loop_scenes(const SceneTable& t, const ListBuffers
     return launch_loop(t, t.n, b, batch, max_iters, s);
 }
 
+void launch_boundary_cell_bounds(const DevParams& P, const float4* b_pos, int* bounds, cudaStream_t s) {
+    if (P.boundary_count) k_boundary_cell_bounds<<<grid_for(P.boundary_count), kBlock, 0, s>>>(P, b_pos, bounds);
+}
+void launch_boundary_zone(const DevParams& P, const float4* b_pos, const int* org, const uint32_t* dim,
+                          unsigned char* zone, cudaStream_t s) {
+    if (P.boundary_count)
+        k_boundary_zone<<<grid_for(P.boundary_count), kBlock, 0, s>>>(P, b_pos, org[0], org[1], org[2], dim[0],
+                                                                      dim[1], zone);
+}
 void launch_boundary_fluid_list(const DevParams& P, const ListBuffers& b, cudaStream_t s) {
     if (P.boundary_count) k_boundary_fluid_list<<<grid_for(P.boundary_count), kBlock, 0, s>>>(P, b);
 }

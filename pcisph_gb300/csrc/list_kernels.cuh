@@ -34,7 +34,23 @@ struct ListBuffers {
                                  // of it at the step's start, walk order, bfl_cap entries chunked over the
                                  // boundary particles (stride boundary_count)
     uint32_t* bfl_count;         // entries per boundary particle; > bfl_cap: walk the fluid buckets
+    // B > 0 (or null): one byte per cell of the box zone_org + [0, zone_dim): 1 where a boundary particle's
+    // cell is within two cells on every axis; a fluid particle whose cell is 0 or outside the box has no
+    // boundary particle within 2h (its boundary terms are zero, none is within r_list)
+    const unsigned char* b_zone;
+    int zone_org[3];
+    uint32_t zone_dim[3];
 };
+
+// Is the cell in the boundary zone (ListBuffers::b_zone)? Cells are the signed integers the reference's
+// floor gives (grid_utils.cl:9-11), held as uint32; the offsets wrap modulo 2^32, which leaves every cell
+// of the box at its offset (a cell far outside may wrap into the box: it then walks, which is exact).
+__device__ __forceinline__ bool in_boundary_zone(const ListBuffers& b, const Cell& c) {
+    const uint32_t ix = c.x - (uint32_t)b.zone_org[0], iy = c.y - (uint32_t)b.zone_org[1],
+                   iz = c.z - (uint32_t)b.zone_org[2];
+    if (ix >= b.zone_dim[0] || iy >= b.zone_dim[1] || iz >= b.zone_dim[2]) return false;
+    return b.b_zone[((size_t)iz * b.zone_dim[1] + iy) * b.zone_dim[0] + ix] != 0;
+}
 
 // One scene: parameters by value; the pressure kernel's last block decides the loop.
 struct OneScene {
@@ -70,6 +86,11 @@ void launch_density_list(const DevParams& P, Control* ctl, const ListBuffers& b,
 // iteration from those lists (walking the fluid buckets when a fast fluid particle is near or a list
 // overflowed). One scene.
 void launch_boundary_fluid_list(const DevParams& P, const ListBuffers& b, cudaStream_t s);
+// The boundary particles' cell bounds (bounds = {min x, y, z, max x, y, z}, preset to INT_MAX / INT_MIN), and
+// the zone map over org + [0, dim) (zeroed by the caller).
+void launch_boundary_cell_bounds(const DevParams& P, const float4* b_pos, int* bounds, cudaStream_t s);
+void launch_boundary_zone(const DevParams& P, const float4* b_pos, const int* org, const uint32_t* dim,
+                          unsigned char* zone, cudaStream_t s);
 void launch_boundary_pressure_list(const DevParams& P, Control* ctl, const ListBuffers& b, cudaStream_t s);
 void launch_normal_list(const DevParams& P, Control* ctl, const ListBuffers& b, cudaStream_t s);
 void launch_force_list(const DevParams& P, Control* ctl, const ListBuffers& b, cudaStream_t s);
