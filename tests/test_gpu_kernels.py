@@ -679,6 +679,30 @@ def test_boundary_lists_change_no_bits(oracle, loop_mode, b_spacing, f_spacing):
             np.testing.assert_array_equal(out[skin][n], w, err_msg=f"skin {skin}: {n}")
 
 
+def test_boundary_zone_changes_no_bits(oracle):
+    """Fluid particles more than two cells from every boundary particle skip the builder's boundary walk
+    (the boundary zone, a byte map over the boundary's cell box). One extra boundary particle 1 km away
+    makes that box too large for a map, so every particle walks; it adds only zero terms, so the fluid's
+    fields are the same bits with and without it."""
+    d = 0.02
+    pos = scenes.lattice_block(10, 12, 10, d, (2 * d, 0.0, 2 * d), seed=23)
+    b_pos = scenes.boundary_box((0.0, 0.0, 0.0), (24 * d, 20 * d, 24 * d), d, layers=2)
+    rng = np.random.default_rng(23)
+    vel = (rng.standard_normal(pos.shape) * 0.05).astype(np.float32)
+    out = []
+    for extra in (False, True):
+        bp = np.concatenate([b_pos, np.array([[1000.0, 1000.0, 1000.0]], np.float32)]) if extra else b_pos
+        p = oracle.derive_params(0.5 * d, 1000.0, pos.shape[0], bp.shape[0], 1e-3, -9.81, 0.2 * d ** 3, 0.5)
+        f = fluid_like(p, min_iters=4, max_iters=4, kernel_variant=2)
+        f.set_fluid_state(pos, vel)
+        f.set_boundary_state(bp)
+        f.step(3)
+        out.append({n: f.get_field(n) for n in ("position", "velocity", "density", "pressure", "pressure_force")})
+        f.close()
+    for n, w in out[0].items():
+        np.testing.assert_array_equal(out[1][n], w, err_msg=n)
+
+
 def test_rederive_after_autotune_keeps_a_valid_sort_scratch():
     """Parameters changed after autotuning re-derive the scene (and the default sort digit width): the next
     steps still sort, with a scratch sized for that width."""
