@@ -49,17 +49,17 @@ STEP_FIXED_BYTES = 340
 CPU_POINTS = 8  # states of the timed run the CPU baseline samples from
 STEP_ITER_BYTES = 136
 DAM_WORKLOADS = {
-    "dam1m": ("config1", "particle-steps/s @1M (<=1% rho err)",
+    "dam1m": ("dam_break_1m", "particle-steps/s @1M (<=1% rho err)",
               "dam break 128x128x64 = 1,048,576 particles, d=0.005 m, dt=2.5e-4 s, reflecting walls, "
               "3-50 corrective iterations to <1% density error"),
-    "dam32k": ("config0", "particle-steps/s @32K (<=1% rho err)",
+    "dam32k": ("dam_break_32k", "particle-steps/s @32K (<=1% rho err)",
                "dam break 32^3 = 32,768 particles, d=0.02 m, dt=1e-3 s, reflecting walls, "
                "3-50 corrective iterations to <1% density error"),
-    "dam1m_boundary": ("config1_boundary", "particle-steps/s @1M with 284K boundary particles (3-7 iterations)",
+    "dam1m_boundary": ("dam_break_1m_boundary", "particle-steps/s @1M with 284K boundary particles (3-7 iterations)",
                        "dam break 128x128x64 = 1,048,576 particles against 284,192 boundary particles (2 layers "
                        "lining a 1.28x0.96x0.32 m box), d=0.005 m, dt=2.5e-4 s, reflecting walls, the reference's "
                        "3-7 corrective iterations (threshold 1%)"),
-    "dam8m": ("config2", "particle-steps/s @8M (<=1% rho err)",
+    "dam8m": ("two_blocks_8m", "particle-steps/s @8M (<=1% rho err)",
               "two 256x128x128 blocks = 8,388,608 particles, d=0.0025 m, dt=1.25e-4 s, reflecting walls, "
               "3-50 corrective iterations to <1% density error"),
 }
@@ -351,7 +351,7 @@ def scenes_workload(args, rank, world, local):
 
     from pcisph_gb300 import Batch, Fluid, build, scenes, setup_scene
     build.build()
-    all_sc = scenes.config3_scenes(count=args.scenes)
+    all_sc = scenes.batch_scenes(count=args.scenes)
     sc = all_sc[rank::world]
     n_total = sum(s.fluid_count for s in sc)
     stream = torch.cuda.Stream()

@@ -419,7 +419,7 @@ __device__ __forceinline__ float pressure_body(const PS& ps, const ListBuffers& 
         auto f = [&](uint32_t j) { acc += density_term(xp.x, xp.y, xp.z, __ldg(&b.pred[j]), P.h2); };
         if (walk) {
             // a batch walks with two gathers in flight (terms still added in walk order): its walkers are
-            // few and latency-bound (config-3 batch over 500 steps 26.8 -> 25.8 s); one scene walks plainly
+            // few and latency-bound (256 batched scenes, 9.8M particles, over 500 steps: 26.8 -> 25.8 s); one scene walks plainly
             // (8M particles all walking: 3.0 ms per sweep, 3.6 with the prefetch)
             if constexpr (PS::kBatched)
                 for_each_neighbour_prefetched(

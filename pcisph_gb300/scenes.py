@@ -97,7 +97,7 @@ def lattice_block(nx, ny, nz, d, origin, seed, jitter=0.05, id_offset=0):
 
 
 def dam_break(n_side=32, seed=0, extent=0.64, box=(1.6, 1.2, 0.8), delta_t=None, steps=1000, **kw):
-    """Config 0/1 dam break: an n_side^3 jittered lattice filling [0, extent]^3 in a box."""
+    """Dam break: an n_side^3 jittered lattice filling [0, extent]^3 in a box (1.6 x 1.2 x 0.8 m)."""
     d = extent / n_side
     if delta_t is None:
         delta_t = 1e-3 * (d / 0.02)
@@ -105,13 +105,13 @@ def dam_break(n_side=32, seed=0, extent=0.64, box=(1.6, 1.2, 0.8), delta_t=None,
     return Scene(f"dam_break_{n_side}^3", pos, d, delta_t, (0.0, 0.0, 0.0), tuple(box), steps=steps, **kw)
 
 
-def config0():
+def dam_break_32k():
     """32,768 particles, d = 0.02 m, dt = 1e-3 s, 1000 steps."""
     return dam_break(32, seed=0, delta_t=1e-3, steps=1000)
 
 
-def config1():
-    """1,048,576 particles, d = 0.005 m, dt = 2.5e-4 s, 500 steps, in the config-0 box.
+def dam_break_1m():
+    """1,048,576 particles, d = 0.005 m, dt = 2.5e-4 s, 500 steps, in the 1.6 x 1.2 x 0.8 m box.
 
     A 128^3 lattice at d = 0.005 m would hold 2,097,152 particles; the workload keeps the stated
     particle count (2^20) and spacing and halves the depth: 128 x 128 x 64 (0.64 x 0.64 x 0.32 m).
@@ -121,8 +121,8 @@ def config1():
     return Scene("dam_break_128x128x64", pos, d, 2.5e-4, (0.0, 0.0, 0.0), (1.6, 1.2, 0.8), steps=500)
 
 
-def config1_boundary():
-    """The config-1 fluid block (1,048,576 particles, d = 0.005 m) against boundary particles: two layers of
+def dam_break_1m_boundary():
+    """The 1,048,576-particle dam-break block (d = 0.005 m) against boundary particles: two layers of
     spacing d lining the floor and four walls of a 1.28 x 0.96 x 0.32 m box (the block fills its left half,
     the whole depth): ~290K boundary particles, the reference's boundary handling at scale (its dambreak
     scene has 154,980 boundary particles for 279,936 fluid ones). The reflecting walls stay on as well.
@@ -139,7 +139,7 @@ def config1_boundary():
                  min_iters=3, max_iters=7)
 
 
-def config2():
+def two_blocks_8m():
     """8,388,608 particles: two 256x128x128 blocks (d = 0.0025 m) at opposite ends of
     [0,1.6]x[0,0.8]x[0,0.4], dt = 1.25e-4 s, 200 steps."""
     d = 0.0025
@@ -150,7 +150,7 @@ def config2():
 
 
 def small_dam(n_side=16, seed=0, **kw):
-    """A small dam break with config-0 physics for tests (same spacing, fewer particles)."""
+    """A small dam break with the 32K dam break's physics for tests (same spacing, fewer particles)."""
     d = 0.02
     return dam_break(n_side, seed=seed, extent=n_side * d, delta_t=1e-3, **kw)
 
@@ -221,8 +221,8 @@ def batch_drop(count, d=0.01, seed=3, id_offset=0, delta_t=1e-3, drop_height=0.5
     return Scene(name, pos, d, delta_t, (0.0, 0.0, 0.0), box_hi)
 
 
-def config3_scenes(count=256, seed=3, n_min=4096, n_max=131072, d=0.01, delta_t=1e-3):
-    """Config 3: `count` scenes with log-uniform particle counts in [n_min, n_max]; each a dam-break block
+def batch_scenes(count=256, seed=3, n_min=4096, n_max=131072, d=0.01, delta_t=1e-3):
+    """Batched scenes: `count` scenes with log-uniform particle counts in [n_min, n_max]; each a dam-break block
     (aspect ratios U[0.5, 2]) or a sphere dropped 0.5 m into a pool holding 30% of its particles."""
     out, offset = [], 0
     ids = np.arange(count, dtype=np.uint64)

@@ -30,9 +30,9 @@ def params_bytes(p):
 def gen_params(R):
     # (particle_radius, rest_density, fluid_count, boundary_count, dt, gravity, viscosity, surface_tension)
     cases = [
-        (0.01, 1000.0, 32768, 0, 1e-3, -9.81, 1.6e-6, 0.5),              # config 0
-        (0.0025, 1000.0, 1048576, 0, 2.5e-4, -9.81, 2.5e-8, 0.5),        # config 1
-        (0.00125, 1000.0, 8388608, 0, 1.25e-4, -9.81, 3.125e-9, 0.5),    # config 2
+        (0.01, 1000.0, 32768, 0, 1e-3, -9.81, 1.6e-6, 0.5),              # 32K dam break
+        (0.0025, 1000.0, 1048576, 0, 2.5e-4, -9.81, 2.5e-8, 0.5),        # 1M dam break
+        (0.00125, 1000.0, 8388608, 0, 1.25e-4, -9.81, 3.125e-9, 0.5),    # 8M two blocks
         (0.5 * 0.7 / 18, 999.972, 279936, 154980, 0.002, -9.81, 8e-5, 1.0),  # reference dambreak
         (0.5 * 0.7 / 19, 999.972, 438976, 322272, 0.002, -9.81, 8e-5, 1.0),  # reference cube_splash
         (0.5 * 0.7 / 30, 999.972, 27000, 0, 0.002, 0.0, 8e-5, 1.0),          # reference simple_drop
@@ -210,7 +210,7 @@ def main(names):
             b_pos0 = scenes.boundary_box((0, 0, 0), (12 * d, 12 * d, 12 * d), d, layers=1)
             gen_scene(R, "step_boundary", sc, b_pos0, 8e-5, 1.0, -9.81, 999.972, 0.05, 2, seed=6)
         elif name == "step_fluid":
-            # fluid only, config-0 physics (no walls in the reference)
+            # fluid only, the 32K dam break's physics (no walls in the reference)
             sc = scenes.small_dam(10, seed=7)
             gen_scene(R, "step_fluid", sc, np.zeros((0, 3), np.float32), 1.6e-6, 0.5, -9.81, 1000.0, 0.05, 2,
                       seed=8)

@@ -88,7 +88,7 @@ def test_magic_modulo_exact(d):
 
 
 def test_scene_configs_are_deterministic():
-    a, b = scenes.config0(), scenes.config0()
+    a, b = scenes.dam_break_32k(), scenes.dam_break_32k()
     assert a.fluid_count == 32768
     np.testing.assert_array_equal(a.fluid_pos, b.fluid_pos)
     assert a.fluid_pos.min() > 0 and a.fluid_pos.max() < 0.64
@@ -96,4 +96,4 @@ def test_scene_configs_are_deterministic():
     assert np.abs(jitter).max() <= 0.05 * 0.02 * 1.0001
     c1 = scenes.dam_break(8, seed=0, extent=0.64)
     assert c1.fluid_count == 512 and abs(c1.spacing - 0.08) < 1e-12
-    assert abs(scenes.config0().viscosity_constant() - 0.2 * 0.02 ** 3) < 1e-15
+    assert abs(scenes.dam_break_32k().viscosity_constant() - 0.2 * 0.02 ** 3) < 1e-15

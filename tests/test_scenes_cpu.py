@@ -5,9 +5,9 @@ from pcisph_gb300 import scenes
 from pcisph_gb300.batch import memory_model
 
 
-def test_config3_scenes_shape_and_determinism():
-    a = scenes.config3_scenes(count=64, seed=3)
-    b = scenes.config3_scenes(count=64, seed=3)
+def test_batch_scenes_shape_and_determinism():
+    a = scenes.batch_scenes(count=64, seed=3)
+    b = scenes.batch_scenes(count=64, seed=3)
     n = np.array([s.fluid_count for s in a])
     assert len(a) == 64
     assert n.min() >= 0.85 * 4096 and n.max() <= 1.1 * 131072
