@@ -15,7 +15,8 @@ iterations until the max density error is below 1%. A "step" is one full PCISPH 
   cpu_baseline  the oracle (CPU port of the reference step) on all host cores, from the same state
   --impl reference  the reference's CPU implementation (the oracle port; the OpenCL runtime the reference
             needs does not exist on these machines) timed on the host cores on the same workload
-With --gpus N > 1 (torchrun) every rank runs its own replica (the step does not shard); value is summed.
+With --gpus N > 1 every rank runs its own replica (the step does not shard); value is summed. Started
+without a launcher, --gpus N > 1 runs this script as N ranks under torch.distributed.run itself.
 """
 import argparse
 import json
@@ -59,7 +60,7 @@ DAM_WORKLOADS = {
                        "dam break 128x128x64 = 1,048,576 particles against 284,192 boundary particles (2 layers "
                        "lining a 1.28x0.96x0.32 m box), d=0.005 m, dt=2.5e-4 s, reflecting walls, the reference's "
                        "3-7 corrective iterations (threshold 1%)"),
-    "dam8m": ("two_blocks_8m", "particle-steps/s @8M (<=1% rho err)",
+    "dam8m": ("two_blocks_8m", "particle-steps/s @8M (3-50 iterations; the scene ends every step at the cap)",
               "two 256x128x128 blocks = 8,388,608 particles, d=0.0025 m, dt=1.25e-4 s, reflecting walls, "
               "3-50 corrective iterations to <1% density error"),
 }
@@ -101,6 +102,28 @@ def parse():
         args.steps = {"dam1m": 500, "dam1m_boundary": 500, "dam32k": 1000, "dam8m": 200,
                       "scenes": 500}.get(args.workload, 200)
     return args
+
+
+def free_port():
+    import socket
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def rank_launch_command(argv, n):
+    """The command that runs this script with arguments argv as n ranks of one node (torch.distributed.run,
+    rendezvous on 127.0.0.1)."""
+    return [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={n}",
+            "--master-addr=127.0.0.1", f"--master-port={free_port()}", os.path.abspath(__file__), *argv]
+
+
+def relaunch_as_ranks(args, argv):
+    """--gpus N > 1 outside a launcher (no WORLD_SIZE): run N ranks and return their exit status; None when
+    this process is already a rank or N = 1."""
+    if args.gpus <= 1 or "WORLD_SIZE" in os.environ:
+        return None
+    return subprocess.call(rank_launch_command(argv, args.gpus))
 
 
 def max_over_ranks(x):
@@ -306,32 +329,40 @@ def cpu_sample_rate(scene, states, seconds, max_steps=None):
     return scene.fluid_count * steps / t_total, steps, float(np.mean(iters))
 
 
+REFERENCE_TIMED_SECONDS = 120.0  # bound of the reference arm's timed steps (its warm-up steps are not bounded)
+
+
 def reference_arm(args, rank, world):
-    """The reference's CPU implementation of the step (the oracle port) on all host cores."""
+    """The reference's CPU implementation of the step (the oracle port) on all host cores: args.warmup
+    untimed steps from the workload's initial state, then up to args.steps timed steps, stopping after
+    REFERENCE_TIMED_SECONDS. Under N ranks rank 0 alone runs it (with every core: a launcher's
+    OMP_NUM_THREADS=1 is overridden before the oracle library loads) and the other ranks exit."""
     if rank != 0:
         return
+    cores = os.cpu_count()
+    os.environ["OMP_NUM_THREADS"] = str(cores)
     from pcisph_gb300 import scenes
     import numpy as np
     cfg, metric, workload = DAM_WORKLOADS.get(args.workload, DAM_WORKLOADS["dam1m"])
     sc = getattr(scenes, cfg)()
     pos, vel = sc.fluid_pos, np.zeros_like(sc.fluid_pos)
-    w = min(args.warmup, 3)
+    w = args.warmup
     if w:
         _, _, _, s = cpu_step_rate(sc, pos, vel, float("inf"), max_steps=w)
         pos, vel = s["f_pos"], s["f_vel"]
-    rate, steps, iters, _ = cpu_step_rate(sc, pos, vel, args.cpu_seconds * 2, max_steps=args.steps)
-    cores = os.cpu_count()
+    rate, steps, iters, _ = cpu_step_rate(sc, pos, vel, REFERENCE_TIMED_SECONDS, max_steps=args.steps)
     line = {
         "impl": "reference", "metric": metric, "value": rate,
-        "unit": "particle-steps/s", "n_gpus": 0, "steps": steps, "warmup": w, "ms_per_step": 1e3 * sc.fluid_count / rate,
+        "unit": "particle-steps/s", "n_gpus": world, "steps": steps, "warmup": w,
+        "ms_per_step": 1e3 * sc.fluid_count / rate,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded jittered lattice)",
         "config": {"workload": workload, "particles": sc.fluid_count, "mean_iterations": iters,
                    "particle_iterations_per_s": rate * iters},
         "cpu_baseline": {"value": rate, "unit": "particle-steps/s", "cores": cores, "kind": "port",
                          "sample": f"{sc.fluid_count} particles x {steps} steps after {w} warm-up steps "
-                                   f"(oracle/pcisph_oracle.cpp, OpenMP over particles; the reference's OpenCL "
-                                   f"runtime is unavailable on this box)"},
+                                   f"(oracle/pcisph_oracle.cpp, OpenMP over particles on {cores} threads; the "
+                                   f"reference's OpenCL runtime is unavailable on this box)"},
         "e2e": {"value": rate, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -389,6 +420,10 @@ def scenes_workload(args, rank, world, local):
     launches = bt.kernel_launches() - launches0
     iters = [(b.total_iterations - a.total_iterations) / args.steps for a, b in zip(st0, st1)]
     batch_loop_iters = max(iters)
+    capped = [int(b.unconverged_steps - a.unconverged_steps) for a, b in zip(st0, st1)]
+    worst = int(np.argmax(capped))
+    worst_state = (bt.get_field(ids[worst], "position", sc[worst].fluid_count),
+                   bt.get_field(ids[worst], "velocity", sc[worst].fluid_count)) if capped[worst] else None
 
     # per-kernel CUDA events over the first timed steps again (profiled host-driven steps, same kernels)
     for i, (p, v) in zip(ids, snap):
@@ -451,6 +486,13 @@ def scenes_workload(args, rank, world, local):
         f.close()
     clocks = sampler.stop()
 
+    gate = {"threshold": max(s.threshold for s in sc), "scene_steps_at_cap": sum(capped),
+            "scene_steps": len(sc) * args.steps, "scenes_with_capped_steps": sum(1 for c in capped if c),
+            "max_density_error": max(b.max_density_error_max for b in st1),
+            "max_density_error_note": "largest end-of-step error of any scene over the warm-up and timed steps",
+            "worst_scene": None}
+    if worst_state is not None:
+        gate["worst_scene"] = capped_scene_vs_oracle(sc[worst], worst_state, capped[worst], local, stream)
     cpu = None
     if rank == 0 and world == 1:  # oracle on the smallest scenes, from the same state, bounded
         order = np.argsort([s.fluid_count for s in sc])[:8]
@@ -484,8 +526,30 @@ def scenes_workload(args, rank, world, local):
             "e2e": {"value": n_total * e2e_steps * world / e2e_s, "unit": "particle-steps/s",
                     "h2d_bytes_per_step": 24 * n_total, "d2h_bytes_per_step": 24 * n_total, "steps": e2e_steps},
             "gpu_launches": launches, "roofline": roof, "kernels": kernels, "cpu_baseline": cpu, "clocks": clocks,
+            "accuracy_gate": gate,
         }
         print(json.dumps(line), flush=True)
+
+
+def capped_scene_vs_oracle(scene, state, capped_steps, device, stream):
+    """The scene whose batched steps most often ended at the iteration cap, stepped once more from its state
+    after the timed steps: through the oracle (the reference's step on the CPU) and through one context of its
+    own, so that the line shows whether the reference's formulation also stops at the cap there."""
+    from pcisph_gb300 import Fluid, setup_scene
+    pos, vel = state
+    O, p, opts = _oracle_for(scene)
+    s = O.new_state(p, pos, vel, scene.boundary_pos)
+    so = O.step(p, opts, s)
+    f = Fluid(device, stream=stream.cuda_stream)
+    setup_scene(f, scene)
+    f.set_fluid_state(pos, vel)
+    f.update()
+    sg = f.stats()
+    f.close()
+    return {"scene": scene.name, "particles": scene.fluid_count, "batched_steps_at_cap": capped_steps,
+            "max_iterations": scene.max_iters,
+            "next_step_oracle": {"iterations": so.iterations, "max_density_error": so.max_err / p.rest_density},
+            "next_step_gpu_alone": {"iterations": sg.iterations, "max_density_error": sg.max_density_error}}
 
 
 SERVE_WORKLOAD = ("Poisson arrivals; particle counts log-uniform in [2,048, 262,144], rollouts U[100, 1000] steps, "
@@ -556,7 +620,12 @@ def serve_workload(args, rank, world, local):
 
 def main():
     args = parse()
+    rc = relaunch_as_ranks(args, sys.argv[1:])
+    if rc is not None:
+        sys.exit(rc)
     rank, world, local = dist_env()
+    if world != args.gpus:
+        sys.exit(f"bench.py: --gpus {args.gpus} but {world} rank(s) were launched")
     if args.impl == "reference":
         reference_arm(args, rank, world)
         return
@@ -704,6 +773,9 @@ def main():
                        "fast_predictions_per_step": (st1.fast_particles - st0.fast_particles) / args.steps,
                        "step_ms_min_median_max": [min(step_ms), statistics.median(step_ms), max(step_ms)],
                        "converged_all_steps": (status_bits & 1) == 0, "status_bits": status_bits,
+                       "accuracy_gate": {"threshold": sc.threshold, "steps_at_cap": int(st1.unconverged_steps),
+                                         "steps": args.steps, "max_density_error": st1.max_density_error_max,
+                                         "all_steps_within": int(st1.unconverged_steps) == 0},
                        "l2": "256 MB written between timed steps (not timed); step working set ~200 MB > L2",
                        "wall_s_timed_loop": wall,
                        "step_algorithmic_bytes_per_particle": step_bytes,

@@ -113,7 +113,9 @@ typedef struct pcisph_step_stats {
                                     half the list skin (the particles near it walked the buckets) */
     uint64_t fast_particles;     /* variant 2: predictions that moved more than half the list skin */
     float list_skin;             /* variant 2: the list skin of the last step, units of h */
-    uint32_t reserved;
+    float max_density_error_max; /* largest end-of-step max_density_error of the steps since the last reset */
+    uint64_t unconverged_steps;  /* steps since the last reset that ended at max_iterations with the density
+                                    variation still above the threshold (status bit 0) */
 } pcisph_step_stats;
 
 /* ----------------------------------------------------------- enums */
@@ -399,9 +401,10 @@ PCISPH_API int pcisph_radixsort_set_digit_bits(pcisph_radixsort* sorter, int bit
  * owns the device's memory, or an allocation would stall a latency-critical loop). No counterpart in the
  * reference. Its scratch is a fixed device array inside this library, reserved on every device that loads
  * the library until the process exits; sorts of more than PCISPH_NOALLOC_SORT_MAX_ELEMENTS keys are
- * rejected with PCISPH_ERR_INVALID_ARG. The first call on a device looks up that array's address (make it
- * before any stream capture). All calls share the array: calls that overlap on the GPU race, so order
- * them on one stream. Keys, values, max_bits and stream as in pcisph_radixsort_enqueue, on the current
+ * rejected with PCISPH_ERR_INVALID_ARG. Every call looks up that array's address in the current context
+ * (nothing is cached, so a re-created context is safe); the first call on a device may load the library's
+ * GPU code there, so make it before any stream capture. All calls share the array: calls that overlap on
+ * the GPU race, so order them on one stream. Keys, values, max_bits and stream as in pcisph_radixsort_enqueue, on the current
  * device. */
 #define PCISPH_NOALLOC_SORT_MAX_ELEMENTS (1u << 20)
 PCISPH_API int pcisph_radixsort_enqueue_noalloc(uint32_t* keys, uint32_t* values, size_t elements,

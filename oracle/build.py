@@ -10,7 +10,9 @@ import subprocess
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "_build", "libpcisph_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libpcisph_ref.so")
-REFERENCE_ROOT = os.environ.get("PCISPH_REFERENCE_DIR", "/root/reference")
+# the reference checkout: $PCISPH_REFERENCE_DIR, else a checkout named "reference" beside this repository
+REFERENCE_ROOT = os.environ.get("PCISPH_REFERENCE_DIR") or os.path.join(os.path.dirname(os.path.dirname(HERE)),
+                                                                         "reference")
 
 CXXFLAGS = ["-std=c++17", "-O3", "-fwrapv", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared"]
 

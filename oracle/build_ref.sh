@@ -11,10 +11,14 @@
 # pipe on the way into g++; no edited copy of any reference file is written.
 # Without it, pcisph.cl:167 would parse as a comma expression and lose gravity.
 #
-# usage: oracle/build_ref.sh [reference_root]   (default: $PCISPH_REFERENCE_DIR or /root/reference)
+# usage: oracle/build_ref.sh <reference_root>   (the checkout holding PCISPH/data/kernels)
 set -euo pipefail
 HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
-REF_ROOT="${1:-${PCISPH_REFERENCE_DIR:-/root/reference}}"
+if [[ $# -ne 1 ]]; then
+    echo "usage: $0 <reference_root>" >&2
+    exit 2
+fi
+REF_ROOT="$1"
 SRC="$REF_ROOT/PCISPH"
 OUT="$HERE/_ref"
 if [[ ! -f "$SRC/data/kernels/pcisph.cl" ]]; then

@@ -58,7 +58,7 @@ class StepStats(C.Structure):
     _fields_ = [("iterations", C.c_int32), ("max_density_error", C.c_float), ("status", C.c_uint32),
                 ("status_all", C.c_uint32), ("steps", C.c_uint64), ("total_iterations", C.c_uint64),
                 ("list_fallbacks", C.c_uint64), ("fast_particles", C.c_uint64), ("list_skin", C.c_float),
-                ("reserved", C.c_uint32)]
+                ("max_density_error_max", C.c_float), ("unconverged_steps", C.c_uint64)]
 
 
 class SceneDesc(C.Structure):

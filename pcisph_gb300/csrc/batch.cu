@@ -736,7 +736,8 @@ int pcisph_batch_scene_stats(pcisph_batch* b, int32_t id, pcisph_step_stats* out
     out->list_fallbacks = c.list_fallbacks;
     out->fast_particles = c.fast_particles;
     out->list_skin = b->adaptive_skin ? skin_level_value((int)c.skin_level) : b->list_skin;
-    out->reserved = 0;
+    out->max_density_error_max = host::float_from_bits(c.max_err_max_bits);
+    out->unconverged_steps = c.unconverged_steps;
     return PCISPH_OK;
 }
 

@@ -63,7 +63,25 @@ struct Control {
     unsigned int any_running;    // batch control: some scene still iterates
     unsigned int skin_level;     // adaptive skin: the level of the current step
     unsigned long long over_level[3];  // adaptive skin: this step's predictions past each level's half skin
+    unsigned long long unconverged_steps;  // steps that ended at max_iters with the variation above threshold
+    unsigned int max_err_max_bits;         // float bits of the largest end-of-step max variation / rest density
 };
+
+// Close a step after its last corrective iteration `it` (Fluid.cpp:301-306 decides the same way): status
+// bit 0 when the step ended above the threshold, and the step's statistics.
+__device__ __forceinline__ void close_step(Control* ctl, unsigned it, float rel, bool converged) {
+    if (!converged) {
+        ctl->status |= 1u;
+        ctl->unconverged_steps += 1;
+    }
+    ctl->status_all |= ctl->status;
+    ctl->iterations_last = (int)it;
+    ctl->max_err_last = rel;
+    // rel >= 0: its bit pattern orders like its value (a NaN variation is flagged by status bit 1)
+    if (rel >= 0.f && __float_as_uint(rel) > ctl->max_err_max_bits) ctl->max_err_max_bits = __float_as_uint(rel);
+    ctl->steps += 1;
+    ctl->total_iters += it;
+}
 
 // List skins (units of h) an adaptive scene chooses from, smallest first.
 constexpr int kSkinLevels = 3;

@@ -17,6 +17,7 @@
 
 #include <algorithm>
 #include <climits>
+#include <cstddef>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -895,7 +896,8 @@ struct pcisph_ctx {
         out->list_fallbacks = host_ctl->list_fallbacks;
         out->fast_particles = host_ctl->fast_particles;
         out->list_skin = opts.list_skin;
-        out->reserved = 0;
+        out->max_density_error_max = host::float_from_bits(host_ctl->max_err_max_bits);
+        out->unconverged_steps = host_ctl->unconverged_steps;
         return PCISPH_OK;
     }
 
@@ -1325,7 +1327,14 @@ int pcisph_restore(pcisph_ctx* ctx, const void* src, size_t src_bytes) {
     if (h.boundary_count)
         rc = pcisph_set_boundary_state(ctx, f + (size_t)h.fluid_count * 8, h.boundary_count, PCISPH_LAYOUT_FLOAT4,
                                        PCISPH_MEM_HOST);
-    return rc;
+    if (rc) return rc;
+    // the step counter continues from the checkpoint's (the other statistics start over)
+    DeviceGuard g(ctx->device);
+    CUDA_TRY(cudaStreamSynchronize(ctx->stream()));
+    const unsigned long long steps = h.steps;
+    CUDA_TRY(cudaMemcpy(reinterpret_cast<unsigned char*>(ctx->ctl) + offsetof(Control, steps), &steps, sizeof steps,
+                        cudaMemcpyHostToDevice));
+    return PCISPH_OK;
 }
 
 int pcisph_autotune(pcisph_ctx* ctx, uint32_t steps, pcisph_tune_result* out) {

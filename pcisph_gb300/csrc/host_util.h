@@ -23,6 +23,13 @@ namespace host {
 
 inline size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 
+// The float whose bit pattern is b (a device-side float kept as bits for atomic max).
+inline float float_from_bits(uint32_t b) {
+    float f;
+    std::memcpy(&f, &b, sizeof f);
+    return f;
+}
+
 inline constexpr float kPi = 3.14159265358979323846f;  // utils/constants.h:4
 inline constexpr uint32_t kListCap = 96;           // neighbour-list entries per particle (multiple of 4)
 inline constexpr uint32_t kNearCap = 64;           // within-h list entries per particle

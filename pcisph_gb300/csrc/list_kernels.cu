@@ -262,14 +262,7 @@ __device__ __forceinline__ void decide(const DevParams& P, Control* ctl) {
     ctl->max_err_bits = 0;
     ctl->blocks_done = 0;
     if (ctl->fast_particles != ctl->fast_at_begin) ctl->list_fallbacks += 1;
-    if (done) {
-        if (!converged) ctl->status |= 1u;
-        ctl->status_all |= ctl->status;
-        ctl->iterations_last = (int)it;
-        ctl->max_err_last = rel;
-        ctl->steps += 1;
-        ctl->total_iters += it;
-    }
+    if (done) close_step(ctl, it, rel, converged);
 }
 
 // pcisph.cl:65-92, and the neighbour list of the step. kBoundary: the scene has boundary particles (their

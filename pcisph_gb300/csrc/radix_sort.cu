@@ -10,8 +10,9 @@ constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
 constexpr int kItems = 16;
 constexpr int kTile = kThreads * kItems;  // 4096 keys per tile
+static_assert(kTile == kRadixTile, "tile size shared with the scratch layout (radix_sort.cuh)");
 
-size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
+constexpr size_t align256(size_t b) { return radix_align256(b); }
 
 // Exclusive scan in place over s[0..count) in shared memory; returns the total. All threads call.
 __device__ uint32_t block_exclusive_scan(uint32_t* s, int count, uint32_t* warp_tmp) {
@@ -92,8 +93,8 @@ __global__ void __launch_bounds__(kThreads) k_scan_rows(uint32_t* __restrict__ c
 
 template <int BITS>
 constexpr size_t downsweep_smem() {
-    return (size_t)kWarps * (1 << BITS) * sizeof(unsigned short) + 2 * (size_t)(1 << BITS) * sizeof(uint32_t) +
-           2 * (size_t)kTile * sizeof(uint32_t);
+    static_assert(kWarps == 8, "radix_downsweep_smem counts 8 warps");
+    return radix_downsweep_smem(BITS);
 }
 
 // Stable rank within the tile, stage in digit order, write each digit run contiguously.
@@ -224,12 +225,6 @@ cudaError_t radix_configure_kernels() {
 
 RadixSorter::~RadixSorter() {
     if (owns_ && scratch_) cudaFree(scratch_);
-}
-
-size_t RadixSorter::scratch_bytes(size_t n, int digit_bits) {
-    const size_t tiles = (n + kTile - 1) / kTile;
-    return 2 * align256(n * sizeof(uint32_t)) + align256(((size_t)1 << digit_bits) * tiles * sizeof(uint32_t)) +
-           align256(((size_t)1 << digit_bits) * sizeof(uint32_t));
 }
 
 void RadixSorter::set_scratch(void* ptr, size_t bytes) {

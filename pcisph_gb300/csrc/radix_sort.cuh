@@ -13,6 +13,26 @@
 
 namespace pcisph {
 
+// Keys per tile of the sort kernels (256 threads x 16 keys).
+constexpr size_t kRadixTile = 4096;
+
+constexpr size_t radix_align256(size_t b) { return (b + 255) & ~size_t(255); }
+
+// Scratch bytes of a sort of n elements with digit_bits-wide digits: alternate keys, alternate values,
+// per-tile digit counts and digit totals, each 256-byte aligned.
+constexpr size_t radix_scratch_bytes(size_t n, int digit_bits) {
+    return 2 * radix_align256(n * sizeof(uint32_t)) +
+           radix_align256(((size_t)1 << digit_bits) * ((n + kRadixTile - 1) / kRadixTile) * sizeof(uint32_t)) +
+           radix_align256(((size_t)1 << digit_bits) * sizeof(uint32_t));
+}
+
+// Dynamic shared memory of the downsweep kernel for bits-wide digits (8 warps' 16-bit digit counters, two
+// digit tables, the tile's keys and values). Above 48 KB the kernel needs radix_configure_kernels().
+constexpr size_t radix_downsweep_smem(int bits) {
+    return (size_t)8 * ((size_t)1 << bits) * sizeof(unsigned short) + 2 * ((size_t)1 << bits) * sizeof(uint32_t) +
+           2 * kRadixTile * sizeof(uint32_t);
+}
+
 // Raise the dynamic shared-memory limit of the wide-digit kernels on the current device.
 // Call once per device before the first sort (outside stream capture).
 cudaError_t radix_configure_kernels();
@@ -31,7 +51,7 @@ class RadixSorter {
     RadixSorter& operator=(const RadixSorter&) = delete;
 
     // Scratch bytes needed for n elements (alternate keys/values + tile counts).
-    static size_t scratch_bytes(size_t n, int digit_bits);
+    static constexpr size_t scratch_bytes(size_t n, int digit_bits) { return radix_scratch_bytes(n, digit_bits); }
     // Use caller-provided scratch (must hold scratch_bytes); otherwise the sorter allocates lazily.
     void set_scratch(void* ptr, size_t bytes);
     void set_digit_bits(int bits) { digit_bits_ = bits; }

@@ -10,12 +10,14 @@
 // the process exits, so it is sized for a modest maximum of PCISPH_NOALLOC_SORT_MAX_ELEMENTS keys
 // (1,048,576 keys: about 8.3 MB per device).
 //
-// Host code cannot use the array's name as a device address (on the host it names a stand-in), so the
-// device address is looked up with cudaGetSymbolAddress once per device, with that device current, on
-// the first call made on that device; make that first call before any stream capture.
+// Host code cannot use the array's name as a device address (on the host it names a stand-in), so every
+// call looks the device address up with cudaGetSymbolAddress on the current device. The lookup allocates
+// nothing and is cheap; it is not cached, because the address belongs to the CUDA context, and a context
+// torn down and created again (cudaDeviceReset) may load the module at another address. The first call on
+// a device may be the one that loads this library's GPU code there; make that first call before any
+// stream capture.
 #include <cuda_runtime.h>
 
-#include <mutex>
 #include <string>
 
 #include "../../include/pcisph_gpu.h"
@@ -29,35 +31,22 @@ namespace {
 
 constexpr size_t kMaxElements = PCISPH_NOALLOC_SORT_MAX_ELEMENTS;
 constexpr int kDigitBits = 8;
-constexpr size_t kTile = 4096;  // keys per tile of the sort kernels (radix_sort.cu)
-constexpr size_t al(size_t b) { return (b + 255) & ~size_t(255); }
-// alternate keys + alternate values + per-tile digit counts + digit totals (RadixSorter::scratch_bytes)
-constexpr size_t kScratchBytes = 2 * al(kMaxElements * 4) +
-                                 al((size_t(1) << kDigitBits) * ((kMaxElements + kTile - 1) / kTile) * 4) +
-                                 al((size_t(1) << kDigitBits) * 4);
+// alternate keys + alternate values + per-tile digit counts + digit totals, as RadixSorter lays them out
+constexpr size_t kScratchBytes = pcisph::RadixSorter::scratch_bytes(kMaxElements, kDigitBits);
+static_assert(kScratchBytes == pcisph::radix_scratch_bytes(kMaxElements, kDigitBits), "scratch layout");
+// this path never raises the kernels' shared-memory limit: the 8-bit downsweep must fit the default 48 KB
+static_assert(pcisph::radix_downsweep_smem(kDigitBits) <= 48 * 1024, "8-bit downsweep exceeds 48 KB");
 
 static __device__ __align__(256) unsigned char g_sort_scratch[kScratchBytes];
 
-std::mutex g_mutex;
-constexpr int kMaxDevices = 256;
-void* g_scratch_addr[kMaxDevices] = {};
-
-// Device address of g_sort_scratch on the current device (looked up once per device).
+// Device address of g_sort_scratch in the current device's context.
 int scratch_for_current_device(void** out) {
-    int dev = -1;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return pcisph::report_error(PCISPH_ERR_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
-    if (dev < 0 || dev >= kMaxDevices) return pcisph::report_error(PCISPH_ERR_INVALID_ARG, "device ordinal out of range");
-    std::lock_guard<std::mutex> lock(g_mutex);
-    if (!g_scratch_addr[dev]) {
-        void* p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_sort_scratch);
-        if (e != cudaSuccess || !p)
-            return pcisph::report_error(PCISPH_ERR_CUDA, std::string("cudaGetSymbolAddress of the sort scratch: ") +
-                                                             cudaGetErrorString(e));
-        g_scratch_addr[dev] = p;
-    }
-    *out = g_scratch_addr[dev];
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_sort_scratch);
+    if (e != cudaSuccess || !p)
+        return pcisph::report_error(PCISPH_ERR_CUDA, std::string("cudaGetSymbolAddress of the sort scratch: ") +
+                                                         cudaGetErrorString(e));
+    *out = p;
     return PCISPH_OK;
 }
 

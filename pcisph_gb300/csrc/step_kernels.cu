@@ -257,14 +257,7 @@ __global__ void __launch_bounds__(kBlock) k_pressure(DevParams P, const uint2* _
         ctl->done = done ? 1u : 0u;
         ctl->max_err_bits = 0;
         ctl->blocks_done = 0;
-        if (done) {
-            if (!converged) ctl->status |= 1u;
-            ctl->status_all |= ctl->status;
-            ctl->iterations_last = (int)it;
-            ctl->max_err_last = rel;
-            ctl->steps += 1;
-            ctl->total_iters += it;
-        }
+        if (done) close_step(ctl, it, rel, converged);
     }
 }
 

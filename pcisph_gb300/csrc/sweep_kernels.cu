@@ -222,14 +222,7 @@ struct OpPressure {
             ctl->done = done ? 1u : 0u;
             ctl->max_err_bits = 0;
             ctl->blocks_done = 0;
-            if (done) {
-                if (!converged) ctl->status |= 1u;
-                ctl->status_all |= ctl->status;
-                ctl->iterations_last = (int)it;
-                ctl->max_err_last = rel;
-                ctl->steps += 1;
-                ctl->total_iters += it;
-            }
+            if (done) close_step(ctl, it, rel, converged);
         }
     }
 };

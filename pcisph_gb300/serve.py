@@ -72,6 +72,9 @@ class Completion:
     status: int         # pcisph_step_status bits seen during the rollout
     position: np.ndarray = None
     velocity: np.ndarray = None
+    unconverged_steps: int = 0      # steps that ended at the iteration cap above the scene's threshold
+    max_density_error: float = 0.0  # largest end-of-step max density variation / rest density
+    threshold: float = 0.01         # the scene's density variation threshold
 
     @property
     def latency(self):
@@ -114,6 +117,7 @@ class _Running:
     arrived: float
     admitted: float
     left: int
+    threshold: float = 0.01
 
 
 @dataclass
@@ -146,7 +150,23 @@ class ServeReport:
             "rollout_s_p50": pct(lat, 50), "rollout_s_p99": pct(lat, 99),
             "queueing_s_p50": pct(que, 50), "queueing_s_p99": pct(que, 99),
             "peak_particles": self.peak_particles, "stalled_steps": len(self.stalled_steps),
+            "accuracy_gate": accuracy_gate(self.completions),
         }
+
+
+def accuracy_gate(completions):
+    """The density-error gate over completed rollouts (the reference's check, Fluid.cpp:301-306, applied to
+    every step): rollouts whose every step ended below the threshold, the scene-steps that ended at the
+    iteration cap above it, and the largest end-of-step error seen."""
+    steps = sum(c.steps for c in completions)
+    capped = sum(c.unconverged_steps for c in completions)
+    return {
+        "rollouts_all_steps_within": sum(1 for c in completions if c.unconverged_steps == 0),
+        "rollouts": len(completions),
+        "scene_steps_at_cap": capped, "scene_steps": steps,
+        "max_density_error": max((c.max_density_error for c in completions), default=0.0),
+        "threshold": max((c.threshold for c in completions), default=0.01),
+    }
 
 
 class Server:
@@ -191,7 +211,7 @@ class Server:
                 break  # FIFO: the head waits for room, the others wait behind it
             self.queue.popleft()
             sid = self.batch.add_scene(req.scene)
-            self.running.append(_Running(req, sid, arrived, now, req.steps))
+            self.running.append(_Running(req, sid, arrived, now, req.steps, float(req.scene.threshold)))
             self.used_bytes += self.cost(req)
             self.used_particles += req.particles
             self._particles[req.rid] = req.particles
@@ -216,7 +236,9 @@ class Server:
             self.used_bytes -= n * self.bpp + self.bps
             self.used_particles -= n
             out.append(Completion(r.req.rid, r.arrived, r.admitted, self.clock_now(), r.req.steps,
-                                  n, int(st.total_iterations), int(st.status_all), pos, vel))
+                                  n, int(st.total_iterations), int(st.status_all), pos, vel,
+                                  int(getattr(st, "unconverged_steps", 0)),
+                                  float(getattr(st, "max_density_error_max", 0.0)), r.threshold))
         self.running = keep
         return out
 

@@ -97,3 +97,28 @@ def test_scene_configs_are_deterministic():
     c1 = scenes.dam_break(8, seed=0, extent=0.64)
     assert c1.fluid_count == 512 and abs(c1.spacing - 0.08) < 1e-12
     assert abs(scenes.dam_break_32k().viscosity_constant() - 0.2 * 0.02 ** 3) < 1e-15
+
+
+def test_ctypes_structs_match_the_c_layout(tmp_path):
+    """Every ctypes mirror in _lib has the size and field offsets the C compiler gives the header's struct
+    (a field added on one side only would shift every later field)."""
+    pairs = [(_lib.SimParams, "pcisph_sim_params"), (_lib.Options, "pcisph_options"),
+             (_lib.StepStats, "pcisph_step_stats"), (_lib.SceneDesc, "pcisph_scene_desc"),
+             (_lib.Camera, "pcisph_camera"), (_lib.TuneResult, "pcisph_tune_result"),
+             (_lib.BatchTuneResult, "pcisph_batch_tune_result"), (_lib.KernelTime, "pcisph_kernel_time")]
+    lines = ['#include <stddef.h>', '#include <stdio.h>', f'#include "{_lib.HEADER}"', "int main(void) {"]
+    for cls, cname in pairs:
+        lines.append(f'printf("{cname} %zu\\n", sizeof({cname}));')
+        for name, *_ in cls._fields_:
+            lines.append(f'printf("{cname}.{name} %zu\\n", offsetof({cname}, {name}));')
+    lines.append("return 0; }")
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-std=c11", "-o", str(exe), str(src)], check=True)
+    got = dict(line.split() for line in subprocess.run([str(exe)], capture_output=True, text=True,
+                                                        check=True).stdout.splitlines())
+    for cls, cname in pairs:
+        assert int(got[cname]) == C.sizeof(cls), cname
+        for name, *_ in cls._fields_:
+            assert int(got[f"{cname}.{name}"]) == getattr(cls, name).offset, (cname, name)

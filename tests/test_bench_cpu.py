@@ -94,3 +94,27 @@ def test_cpu_sample_rate_steps_every_state():
     assert steps == 1 and rate > 0 and sc.min_iters <= iters <= sc.max_iters
     rate, steps, iters = bench.cpu_sample_rate(sc, states, seconds=0.05)
     assert steps >= 1 and rate > 0
+
+
+def test_gpus_flag_launches_that_many_ranks():
+    """`bench.py --gpus 2` started without a launcher runs itself as two ranks (torch.distributed.run on
+    127.0.0.1); the reference arm runs on rank 0 alone and reports the launch's world size."""
+    import json
+    import subprocess
+    out = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--gpus", "2",
+                          "--workload", "dam32k", "--steps", "1", "--warmup", "0"],
+                         capture_output=True, text=True, timeout=900, cwd=ROOT)
+    assert out.returncode == 0, out.stderr[-2000:]
+    lines = [json.loads(l) for l in out.stdout.splitlines() if l.startswith("{")]
+    assert len(lines) == 1, out.stdout
+    line = lines[0]
+    assert line["n_gpus"] == 2 and line["impl"] == "reference" and line["steps"] == 1
+    assert line["cpu_baseline"]["cores"] == os.cpu_count()
+
+
+def test_rank_launch_command():
+    import bench
+    cmd = bench.rank_launch_command(["--gpus", "4", "--steps", "2"], 4)
+    assert cmd[1:3] == ["-m", "torch.distributed.run"]
+    assert "--nproc-per-node=4" in cmd and "--master-addr=127.0.0.1" in cmd
+    assert cmd[-3:] == ["--gpus", "4", "--steps", "2"][-3:] and cmd[-5].endswith("bench.py")

@@ -1,0 +1,182 @@
+"""GPU parity at the sizes the benchmark runs: the library's default step against the oracle.
+
+The oracle (oracle/pcisph_oracle.cpp) restates the reference step (Fluid.cpp:176-316 and the kernels of
+pcisph.cl:65-300) on the CPU; it is pinned bit for bit to the reference's own kernels by
+tests/test_oracle_golden.py. Each test runs the configuration the benchmark times -- kernel variant 2
+(neighbour lists), the spatial working order where the library chooses it, the step's graph with its
+device-side loop decision -- and the oracle from the same positions and velocities, and compares:
+
+  cell keys, the stable permutation (src) and the cell ranges: bit-exact;
+  density, normal, other force, pressure force, position: within RTOL = 1e-5 normwise (gpu_util);
+  pressure and density variation, which cancel rho* - rho0: within 1e-5 of their terms' scale;
+  velocity: within 1e-5 normwise, or, where the step's velocity change cancels (a block at rest whose
+    pressure force balances gravity), within 3x the FP32 oracle's own error against its FP64 rerun;
+  the corrective iteration count: equal.
+
+Sizes: the 32,768-particle dam break (its first step, and a step after ten steps in one context, which
+reuses the bucket placement of an earlier step); the 1,048,576-particle dam break (one step from the state
+after the benchmark's three warm-up steps: two-pass 10-bit sort, real neighbour counts against the list
+caps); the 8,388,608-particle two-block scene (22-bit keys in three sort passes: keys, permutation, cell
+ranges, reordered positions and the density sweep); and a batch of scenes shaped like the batched
+workload's (a sphere dropped into a pool, a dam block, a small block).
+"""
+import numpy as np
+import pytest
+
+from gpu_util import RTOL, rel_err
+from oracle.oracle import make_options
+from pcisph_gb300 import Batch, Fluid, scenes, setup_scene
+
+pytestmark = pytest.mark.gpu
+
+
+def _oracle_params(oracle, sc):
+    p = oracle.derive_params(sc.particle_radius, sc.rest_density, sc.fluid_count, 0, sc.delta_t, sc.gravity,
+                             sc.viscosity_constant(), sc.surface_tension)
+    opts = make_options(threshold=sc.threshold, min_iters=sc.min_iters, max_iters=sc.max_iters, walls=sc.walls,
+                        box_lo=sc.box_lo, box_hi=sc.box_hi, restitution=sc.restitution)
+    return p, opts
+
+
+def _oracle_step(oracle, sc, pos, vel, fp64=True):
+    """One oracle step from (pos, vel) in FP32, and in FP64 when asked: (params, fp32 state, fp32 stats,
+    fp64 state or None, fp64 stats or None)."""
+    p, opts = _oracle_params(oracle, sc)
+    s32 = oracle.new_state(p, pos, vel)
+    st32 = oracle.step(p, opts, s32)
+    s64 = st64 = None
+    if fp64:
+        s64 = oracle.new_state(p, pos, vel, dtype=np.float64)
+        st64 = oracle.step(p, opts, s64)
+    return p, s32, st32, s64, st64
+
+
+FIELDS = [("density", "f_rho"), ("normal", "f_normal"), ("other_force", "f_other"),
+          ("pressure_force", "f_fpress"), ("position", "f_pos"), ("velocity", "f_vel"), ("pressure", "f_press"),
+          ("density_variation", "f_err")]
+
+
+def _scale(p, name, iterations):
+    if name == "pressure":
+        return p.density_variation_scaling_factor * p.rest_density * iterations
+    if name == "density_variation":
+        return p.rest_density
+    return None
+
+
+def _compare_step(label, get, stats, p, s32, st32, s64=None, st64=None):
+    """Compare a GPU step (get(name) reads a field in sorted order) with the oracle's step."""
+    assert stats.iterations == st32.iterations, (label, "iterations", stats.iterations, st32.iterations)
+    eq = np.testing.assert_array_equal
+    if get("keys") is not None:
+        eq(get("keys"), s32["f_keys"], err_msg=f"{label}: keys")
+        eq(get("src"), s32["f_src"], err_msg=f"{label}: src")
+        eq(get("cell_offsets"), s32["f_off"], err_msg=f"{label}: cell ranges")
+    errs, bounds = {}, {}
+    same_iters64 = st64 is not None and st64.iterations == st32.iterations
+    for name, key in FIELDS:
+        sc = _scale(p, name, st32.iterations)
+        errs[name] = rel_err(get(name), s32[key], sc)
+        bounds[name] = RTOL
+        if name == "velocity" and same_iters64:
+            own = rel_err(s32[key], s64[key], sc)  # the FP32 oracle's own error
+            bounds[name] = max(RTOL, 3 * own)
+    print(label, f"iterations {st32.iterations}",
+          {k: f"{v:.1e} (<= {bounds[k]:.1e})" for k, v in errs.items()})
+    bad = {k: v for k, v in errs.items() if not v <= bounds[k]}
+    assert not bad, (label, bad, bounds)
+
+
+def _fluid(sc):
+    f = Fluid(0)
+    setup_scene(f, sc)  # the library defaults: kernel variant 2, working order by size, graph loop
+    return f
+
+
+def _ctx_getter(f):
+    return lambda name: f.get_field(name)
+
+
+def test_dam_break_32k_first_step(oracle):
+    sc = scenes.dam_break_32k()
+    vel = np.zeros_like(sc.fluid_pos)
+    f = _fluid(sc)
+    f.update()
+    _compare_step("32K step 1", _ctx_getter(f), f.stats(), *_oracle_step(oracle, sc, sc.fluid_pos, vel))
+    f.close()
+
+
+def test_dam_break_32k_step_after_ten(oracle):
+    """The eleventh step of one context (bucket placement from an earlier step reused) against the oracle
+    stepped once from that context's state."""
+    sc = scenes.dam_break_32k()
+    f = _fluid(sc)
+    f.step(10)
+    pos, vel = f.get_field("position"), f.get_field("velocity")
+    f.update()
+    _compare_step("32K step 11", _ctx_getter(f), f.stats(), *_oracle_step(oracle, sc, pos, vel))
+    f.close()
+
+
+def test_dam_break_1m_warmed_step(oracle):
+    sc = scenes.dam_break_1m()
+    f = _fluid(sc)
+    f.step(3)  # the benchmark's warm-up
+    pos, vel = f.get_field("position"), f.get_field("velocity")
+    f.update()
+    _compare_step("1M step 4", _ctx_getter(f), f.stats(), *_oracle_step(oracle, sc, pos, vel))
+    f.close()
+
+
+def test_two_blocks_8m_sort_and_density(oracle):
+    sc = scenes.two_blocks_8m()
+    p, _ = _oracle_params(oracle, sc)
+    assert p.bucket_count == 4194304 and oracle.sort_bit_count(p.bucket_count) == 22
+    f = _fluid(sc)
+    f.run_stage("sort")
+    keys, ids = oracle.initialize(p, sc.fluid_pos)
+    order = np.argsort(keys, kind="stable")  # the stable sort's contract: ties by ascending id
+    eq = np.testing.assert_array_equal
+    eq(f.get_field("keys"), keys[order])
+    eq(f.get_field("src"), ids[order])
+    spos, _, off = oracle.reorder(keys[order], ids[order], sc.fluid_pos, None, p.bucket_count)
+    eq(f.get_field("cell_offsets"), off)
+    eq(f.get_field("sorted_position"), spos)
+    f.run_stage("density")
+    rho = oracle.update_density(p, np.zeros(2 * p.bucket_count, np.uint32), np.zeros((0, 3), np.float32), off,
+                                spos)
+    e = rel_err(f.get_field("density"), rho)
+    print(f"8M density: {e:.1e}")
+    assert e <= RTOL
+    f.close()
+
+
+def test_batched_scene_shapes_vs_oracle(oracle):
+    """Scenes shaped like the batched workload's in one batch: each scene's first step against the oracle,
+    then twenty steps against the same scene in a context of its own (bit for bit)."""
+    drop = scenes.batch_drop(30000, d=0.01, seed=31, name="drop30k")
+    dam = scenes.batch_dam(30000, 1.4, 0.8, d=0.01, seed=32, name="dam30k")
+    small = scenes.batch_dam(4096, 0.7, 1.6, d=0.01, seed=33, name="dam4k")
+    sc = [drop, dam, small]
+    bt = Batch(0, max_particles=sum(s.fluid_count for s in sc) + 64, max_scenes=4)
+    ids = [bt.add_scene(s) for s in sc]
+    bt.step(1)
+    bt.sync()
+    for s, i in zip(sc, ids):
+        vel = np.zeros_like(s.fluid_pos)
+        _compare_step(f"batch {s.name} step 1", lambda name, s=s, i=i: (
+            None if name in ("keys", "src", "cell_offsets") else bt.get_field(i, name, s.fluid_count)),
+            bt.stats(i), *_oracle_step(oracle, s, s.fluid_pos, vel))
+    bt.step(19)
+    bt.sync()
+    for s, i in zip(sc, ids):
+        f = Fluid(0)
+        setup_scene(f, s, kernel_variant=2)
+        f.step(20)
+        for name in ("position", "velocity", "density", "pressure"):
+            np.testing.assert_array_equal(bt.get_field(i, name, s.fluid_count), f.get_field(name),
+                                          err_msg=f"{s.name}: {name}")
+        a, b = bt.stats(i), f.stats()
+        assert (a.iterations, a.steps, a.total_iterations) == (b.iterations, b.steps, b.total_iterations)
+        f.close()
+    bt.close()

@@ -468,13 +468,16 @@ def test_snapshot_restore_continues_exactly(tmp_path, golden, case):
     f.step(5)
     want = {n: f.get_field(n) for n in ("position", "velocity", "density", "pressure")}
     iters = f.stats().iterations
+    steps = f.stats().steps
     f.close()
     h = Fluid(0)
     h.load(path)
+    assert h.stats().steps == steps - 5  # the step counter is part of the checkpoint
     h.step(5)
     for n, w in want.items():
         np.testing.assert_array_equal(h.get_field(n), w, err_msg=n)
     assert h.stats().iterations == iters
+    assert h.stats().steps == steps
     with pytest.raises(PcisphError):
         h.restore(b"PCSN" + bytes(10))
     h.close()

@@ -15,7 +15,9 @@ class FakeBatch:
     class Stats:
         def __init__(self, steps):
             self.total_iterations = 3 * steps
-            self.status_all = 0
+            self.status_all = 1 if steps >= 8 else 0  # 8-step rollouts end one step at the cap
+            self.unconverged_steps = 1 if steps >= 8 else 0
+            self.max_density_error_max = 0.02 if steps >= 8 else 0.009
 
     def __init__(self, budget, bpp, bps):
         self.live = {}      # sid -> [particles, steps taken]
@@ -81,6 +83,11 @@ def test_every_request_runs_exactly_its_steps_within_budget(realtime):
     assert not fb.live and rep.running_at_end == 0 and rep.queued_at_end == 0
     s = rep.summary()
     assert s["completed"] == len(reqs) and s["particle_steps_per_s"] > 0
+    capped = sum(1 for r in reqs if r.steps >= 8)
+    assert 0 < capped < len(reqs)
+    assert s["accuracy_gate"] == {"rollouts_all_steps_within": len(reqs) - capped, "rollouts": len(reqs),
+                                  "scene_steps_at_cap": capped, "scene_steps": sum(r.steps for r in reqs),
+                                  "max_density_error": 0.02, "threshold": pytest.approx(0.01)}
 
 
 def test_oversized_requests_are_rejected_and_scene_limit_holds():
