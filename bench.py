@@ -589,6 +589,9 @@ def serve_workload(args, rank, world, local):
     clocks = sampler.stop()
     summ = rep.summary()
     summ["graph_instantiations"], summ["graph_updates"] = bt.graph_stats()
+    bt.close()
+    # the same request mix stepped as one context per request against one batch of those requests
+    summ["per_scene_vs_batched"] = request_mix_comparison(reqs[:SERVE_MIX_SCENES], SERVE_MIX_STEPS, local, stream)
     if world > 1:
         got = [None] * world
         dist.all_gather_object(got, summ)
@@ -615,7 +618,54 @@ def serve_workload(args, rank, world, local):
             "clocks": clocks,
         }
         print(json.dumps(line), flush=True)
+
+
+SERVE_MIX_SCENES = 64  # requests of the mix comparison (the first ones of the arrival order)
+SERVE_MIX_STEPS = 20   # time steps each of them takes in both forms
+
+
+def request_mix_comparison(requests, steps, device, stream):
+    """Scenes of `requests` advanced `steps` time steps, once with one context per request (each context's
+    step launched in turn, the plain step per scene) and once as one batch: particle-steps/s and scene-steps/s
+    of both, on the same stream. The rate a served rollout mix reaches is bounded by the second form."""
+    import torch
+
+    from pcisph_gb300 import Batch, Fluid, setup_scene
+    scs = [r.scene for r in requests]
+    n = sum(s.fluid_count for s in scs)
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(steps):
+            fn()
+        b.record(stream)
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / 1e3
+
+    ctxs = []
+    for s in scs:
+        f = Fluid(device, stream=stream.cuda_stream)
+        setup_scene(f, s)
+        f.update()  # first step (graph instantiation) untimed
+        ctxs.append(f)
+    t_single = timed(lambda: [f.update() for f in ctxs])
+    for f in ctxs:
+        f.close()
+    bt = Batch(device, max_particles=n, max_scenes=len(scs), stream=stream.cuda_stream)
+    for s in scs:
+        bt.add_scene(s)
+    bt.step(1)
+    t_batch = timed(lambda: bt.step(1))
     bt.close()
+    for r in requests:
+        r.release()
+    return {"scenes": len(scs), "particles": n, "steps": steps,
+            "per_scene_contexts": {"particle_steps_per_s": n * steps / t_single,
+                                   "scene_steps_per_s": len(scs) * steps / t_single},
+            "batched": {"particle_steps_per_s": n * steps / t_batch, "scene_steps_per_s": len(scs) * steps / t_batch},
+            "speedup_of_batch": t_single / t_batch}
 
 
 def main():

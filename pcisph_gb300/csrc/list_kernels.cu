@@ -94,6 +94,15 @@ __device__ __forceinline__ void list_finish(uint32_t* list, uint32_t i, uint32_t
     if (n <= cap && (n & 7u)) list_store_chunk(list, i, n >> 3, stride, buf);
 }
 
+// One float4 of data that the step's kernels write: the read-only path, or (kCoherent) a plain load for data
+// that other blocks of the same launch wrote before a grid barrier (the persistent loop), which the
+// read-only path may serve stale.
+template <bool kCoherent>
+__device__ __forceinline__ float4 load_slot(const float4* p) {
+    if constexpr (kCoherent) return *p;
+    else return __ldg(p);
+}
+
 // Call f(j) for the n listed neighbours of particle i in list order. The next chunk's indices are loaded
 // while the current chunk's eight gathers are in flight, so the list stream and the gathers overlap. The
 // list loads are streaming (evict-first): the lists do not push the gathered particle data out of L2.
@@ -228,6 +237,7 @@ __global__ void __launch_bounds__(kBlock) k_boundary_zone(DevParams P, const flo
 // pcisph.cl:212-263 with boundary_update = 1 from boundary particle k's fluid list: a fluid particle not
 // listed was farther than r_list from x_b at the step's start, so it is farther than h from x_b at its
 // prediction unless it moved more than half the skin, which flags its bucket (then k walks).
+template <bool kCoherent = false>
 __device__ __forceinline__ void boundary_pressure_list_body(const DevParams& P, const Control* ctl,
                                                             const ListBuffers& b, uint32_t k) {
     if (k >= P.boundary_count) return;
@@ -240,7 +250,7 @@ __device__ __forceinline__ void boundary_pressure_list_body(const DevParams& P, 
         c = cell_of(xb.x, xb.y, xb.z, P);
         walk = walk || near_fast(P, b.bucket_fast, c);
     }
-    auto f = [&](uint32_t j) { boundary_density_term(xb, __ldg(&b.pred[j]), P.h2, acc); };
+    auto f = [&](uint32_t j) { boundary_density_term(xb, load_slot<kCoherent>(&b.pred[j]), P.h2, acc); };
     if (walk) for_each_neighbour(b.cells, c, P, f);
     else for_each_listed(b.bfl, k, cnt, P.boundary_count, f);
     boundary_pressure_finish(P, xb, acc, b.b_press, const_cast<float4*>(b.bpf), k);
@@ -375,7 +385,7 @@ __global__ void __launch_bounds__(kBlock) k_force_list(PS ps, ListBuffers b) {
 
 // pcisph.cl:212-263 (boundary_update = 0); one scene: also the stop decision in the last block
 // One particle's pressure sweep; returns its density variation (0 when skipped or out of range).
-template <class PS>
+template <class PS, bool kCoherent = false>
 __device__ __forceinline__ float pressure_body(const PS& ps, const ListBuffers& b, uint32_t i) {
     float dv = 0.f;
     if (i < ps.count() && !ps.skip_pressure(i)) {
@@ -409,14 +419,14 @@ __device__ __forceinline__ float pressure_body(const PS& ps, const ListBuffers& 
         auto fb = [&](uint32_t j) { acc += density_term(xp.x, xp.y, xp.z, __ldg(&b.b_pos[j]), P.h2); };
         if (walk_boundary) for_each_neighbour(b.b_cells, c, P, fb);
         else if (list_boundary) for_each_listed(b.bnbr, i, bcnt, b.nbr_stride, fb);
-        auto f = [&](uint32_t j) { acc += density_term(xp.x, xp.y, xp.z, __ldg(&b.pred[j]), P.h2); };
+        auto f = [&](uint32_t j) { acc += density_term(xp.x, xp.y, xp.z, load_slot<kCoherent>(&b.pred[j]), P.h2); };
         if (walk) {
             // a batch walks with two gathers in flight (terms still added in walk order): its walkers are
             // few and latency-bound (256 batched scenes, 9.8M particles, over 500 steps: 26.8 -> 25.8 s); one scene walks plainly
             // (8M particles all walking: 3.0 ms per sweep, 3.6 with the prefetch)
             if constexpr (PS::kBatched)
                 for_each_neighbour_prefetched(
-                    b.cells, c, P, [&](uint32_t j) { return __ldg(&b.pred[j]); },
+                    b.cells, c, P, [&](uint32_t j) { return load_slot<kCoherent>(&b.pred[j]); },
                     [&](uint32_t, const float4& o) { acc += density_term(xp.x, xp.y, xp.z, o, P.h2); });
             else
                 for_each_neighbour(b.cells, c, P, f);
@@ -471,7 +481,7 @@ __global__ void __launch_bounds__(BS) k_pressure_list(PS ps, ListBuffers b) {
 // pcisph.cl:265-300, then predict (pcisph.cl:175-193) or integrate with optional walls
 // One particle's pressure-force sweep, then predict (mode 0 before the decision, 1) or integrate (mode 0
 // after it, 2) with optional walls.
-template <class PS>
+template <class PS, bool kCoherent = false>
 __device__ __forceinline__ void pressure_force_body(const PS& ps, const ListBuffers& b, uint32_t i, int mode) {
     if (i >= ps.count() || ps.skip_force(i)) return;
     const DevParams& P = ps.params(i);
@@ -487,10 +497,10 @@ __device__ __forceinline__ void pressure_force_body(const PS& ps, const ListBuff
     const bool walk_boundary = near_b && !list_boundary;
     Cell c{0u, 0u, 0u};
     if (cnt > P.near_cap || walk_boundary) c = cell_of(xi.x, xi.y, xi.z, P);
-    auto fb = [&](uint32_t j) { pressure_force_term(xi, __ldg(&b.bpf[j]), P.h, P.h2, f); };
+    auto fb = [&](uint32_t j) { pressure_force_term(xi, load_slot<kCoherent>(&b.bpf[j]), P.h, P.h2, f); };
     if (walk_boundary) for_each_neighbour(b.b_cells, c, P, fb);
     else if (list_boundary) for_each_listed(b.bnbr, i, bcnt, b.nbr_stride, fb);
-    auto body = [&](uint32_t j) { pressure_force_term(xi, __ldg(&b.pf4[j]), P.h, P.h2, f); };
+    auto body = [&](uint32_t j) { pressure_force_term(xi, load_slot<kCoherent>(&b.pf4[j]), P.h, P.h2, f); };
     if (cnt <= P.near_cap) for_each_listed(b.near, i, cnt, b.nbr_stride, body);
     else for_each_neighbour(b.cells, c, P, body);
     const float m = P.particle_mass;
@@ -558,11 +568,12 @@ __global__ void __launch_bounds__(kBlock) k_corrective_loop(PS ps, ListBuffers b
         if constexpr (!PS::kBatched) {  // boundary pressures at the predicted positions (read by the force)
             const DevParams& P = ps.params(0);
             for (uint32_t k = blockIdx.x * kBlock + threadIdx.x; k < P.boundary_count; k += stride)
-                boundary_pressure_list_body(P, ps.control(0), b, k);
+                boundary_pressure_list_body<true>(P, ps.control(0), b, k);
         }
         unsigned local = 0;
         for (uint32_t r = 0; r < rounds; ++r)
-            local = max(local, __float_as_uint(pressure_body(ps, b, r * stride + blockIdx.x * kBlock + threadIdx.x)));
+            local = max(local, __float_as_uint(
+                                   pressure_body<PS, true>(ps, b, r * stride + blockIdx.x * kBlock + threadIdx.x)));
         if (!PS::kBatched) {  // batched scenes reduced per scene inside the body
             const unsigned m = __reduce_max_sync(0xffffffffu, local);
             if ((threadIdx.x & 31) == 0 && m) atomicMax(&ps.control(0)->max_err_bits, m);
@@ -596,7 +607,8 @@ __global__ void __launch_bounds__(kBlock) k_corrective_loop(PS ps, ListBuffers b
             }
         }
         grid.sync();
-        for (uint32_t r = 0; r < rounds; ++r) pressure_force_body(ps, b, r * stride + blockIdx.x * kBlock + threadIdx.x, 0);
+        for (uint32_t r = 0; r < rounds; ++r)
+            pressure_force_body<PS, true>(ps, b, r * stride + blockIdx.x * kBlock + threadIdx.x, 0);
         grid.sync();
         if (*reinterpret_cast<volatile unsigned*>(&loop->any_running) == 0u) break;
     }

@@ -7,11 +7,16 @@ tests/test_oracle_golden.py. Each test runs the configuration the benchmark time
 device-side loop decision -- and the oracle from the same positions and velocities, and compares:
 
   cell keys, the stable permutation (src) and the cell ranges: bit-exact;
-  density, normal, other force, pressure force, position: within RTOL = 1e-5 normwise (gpu_util);
-  pressure and density variation, which cancel rho* - rho0: within 1e-5 of their terms' scale;
-  velocity: within 1e-5 normwise, or, where the step's velocity change cancels (a block at rest whose
-    pressure force balances gravity), within 3x the FP32 oracle's own error against its FP64 rerun;
-  the corrective iteration count: equal.
+  the corrective iteration count: equal;
+  every FP32 field (density, normal, other force, pressure, density variation, pressure force, position,
+    velocity): within RTOL = 1e-5 normwise of the FP32 oracle (pressure and density variation, which cancel
+    rho* - rho0, on the scale of their terms), or else no farther from the oracle's FP64 rerun of the same
+    step than max(RTOL, 3x the FP32 oracle's own distance from it). The second branch covers two measured
+    cases: fields that carry a whole step's corrective loop (pressure force and velocity after 7-27
+    iterations drift to ~5e-5 in the FP32 oracle itself), and pairs at r = h, where the reference's
+    curvature force (pcisph.cl:121-173) jumps and the FP32 oracle's sqrtf(r^2) lands on the other side of
+    the cut-off from the FP64 rerun (at 1M, 4 particles give the FP32 oracle a 6.9e-4 other-force error
+    against FP64; the GPU is within 3e-7 of FP64 there).
 
 Sizes: the 32,768-particle dam break (its first step, and a step after ten steps in one context, which
 reuses the bucket placement of an earlier step); the 1,048,576-particle dam break (one step from the state
@@ -72,19 +77,25 @@ def _compare_step(label, get, stats, p, s32, st32, s64=None, st64=None):
         eq(get("keys"), s32["f_keys"], err_msg=f"{label}: keys")
         eq(get("src"), s32["f_src"], err_msg=f"{label}: src")
         eq(get("cell_offsets"), s32["f_off"], err_msg=f"{label}: cell ranges")
-    errs, bounds = {}, {}
     same_iters64 = st64 is not None and st64.iterations == st32.iterations
+    report, bad = {}, {}
     for name, key in FIELDS:
         sc = _scale(p, name, st32.iterations)
-        errs[name] = rel_err(get(name), s32[key], sc)
-        bounds[name] = RTOL
-        if name == "velocity" and same_iters64:
-            own = rel_err(s32[key], s64[key], sc)  # the FP32 oracle's own error
-            bounds[name] = max(RTOL, 3 * own)
-    print(label, f"iterations {st32.iterations}",
-          {k: f"{v:.1e} (<= {bounds[k]:.1e})" for k, v in errs.items()})
-    bad = {k: v for k, v in errs.items() if not v <= bounds[k]}
-    assert not bad, (label, bad, bounds)
+        got = get(name)
+        e32 = rel_err(got, s32[key], sc)
+        if e32 <= RTOL:
+            report[name] = f"{e32:.1e}"
+            continue
+        if not same_iters64:
+            bad[name] = (e32, "FP64 rerun took other iteration counts")
+            continue
+        e64 = rel_err(got, s64[key], sc)
+        own = rel_err(s32[key], s64[key], sc)  # the FP32 oracle's own distance from FP64
+        report[name] = f"{e32:.1e} (vs FP64 {e64:.1e}, FP32 oracle vs FP64 {own:.1e})"
+        if not e64 <= max(RTOL, 3 * own):
+            bad[name] = (e32, e64, own)
+    print(label, f"iterations {st32.iterations}", report)
+    assert not bad, (label, bad)
 
 
 def _fluid(sc):
