@@ -38,31 +38,13 @@
 
 #include "list_kernels.cuh"
 #include "pair_terms.cuh"
+#include "sweep_device.cuh"
 
 namespace pcisph {
 namespace {
 
 constexpr int kBlock = 256;
 inline unsigned grid_for(uint32_t n) { return (n + kBlock - 1) / kBlock; }
-
-// atomicMax aggregated over the lanes of a warp that target the same address (one atomic per address).
-__device__ __forceinline__ void warp_atomic_max(unsigned* addr, unsigned v) {
-    const unsigned act = __activemask();
-    const unsigned peers = __match_any_sync(act, (unsigned long long)addr);
-    const unsigned m = __reduce_max_sync(peers, v);
-    if ((int)(threadIdx.x & 31) == __ffs(peers) - 1) atomicMax(addr, m);
-}
-
-// Add the number of this warp's lanes with pred set to *addr: one atomic per group of lanes sharing addr,
-// none when no lane has pred.
-__device__ __forceinline__ void warp_count(unsigned long long* addr, bool pred) {
-    const unsigned act = __activemask();
-    const unsigned set = __ballot_sync(act, pred);
-    if (!set) return;
-    const unsigned peers = __match_any_sync(act, (unsigned long long)addr);
-    const unsigned c = __popc(set & peers);
-    if (c && (int)(threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(addr, (unsigned long long)c);
-}
 
 // List layout: entries k = 8c .. 8c+7 of particle i (chunk c) are 32 contiguous bytes at uint4 offset
 // 2 (c * stride + i); chunks are column-major over particles. A warp's 32 consecutive particles read
@@ -129,27 +111,6 @@ __device__ __forceinline__ void for_each_listed(const uint32_t* __restrict__ lis
             if ((uint32_t)u < left) f(e[u]);
         a = na;
         b = nb;
-    }
-}
-
-// After predicting x*_i (stored as xs): a fast particle (moved more than half the skin) flags its bucket
-// and is counted (one atomic per warp that has one; no store otherwise: in a splash most predictions are
-// fast, and a flag stored by each of their warps measured slower than the counts alone); the predictions
-// past each adaptive skin level are counted.
-__device__ __forceinline__ void note_displacement(const DevParams& P, Control* ctl,
-                                                  unsigned char* __restrict__ bucket_fast, const float4& xi,
-                                                  const float4& xs) {
-    const float dx = xs.x - xi.x, dy = xs.y - xi.y, dz = xs.z - xi.z;  // exact: xs and xi are close
-    const float disp = sqrtf(dist2(dx, dy, dz));
-    const bool fast = disp > P.list_half_skin;
-    warp_count(&ctl->fast_particles, fast);
-    if (P.adaptive_skin) {
-#pragma unroll
-        for (int k = 0; k < kSkinLevels; ++k) warp_count(&ctl->over_level[k], disp > P.skin_half[k]);
-    }
-    if (fast) {
-        const Cell c = cell_of(xi.x, xi.y, xi.z, P);
-        bucket_fast[P.bucket_base + hash_key(c.x, c.y, c.z, P)] = 1;
     }
 }
 
@@ -258,21 +219,6 @@ __device__ __forceinline__ void boundary_pressure_list_body(const DevParams& P, 
 
 __global__ void __launch_bounds__(kBlock) k_boundary_pressure_list(DevParams P, const Control* ctl, ListBuffers b) {
     boundary_pressure_list_body(P, ctl, b, blockIdx.x * kBlock + threadIdx.x);
-}
-
-// The loop decision of one scene after its pressure sweep (Fluid.cpp:284-306).
-__device__ __forceinline__ void decide(const DevParams& P, Control* ctl) {
-    const float mx = __uint_as_float(ctl->max_err_bits);
-    const unsigned it = ctl->iter + 1;
-    const float rel = mx / P.rest_density;
-    const bool converged = rel < P.threshold;
-    const bool done = it >= (unsigned)P.max_iters || (it >= (unsigned)P.min_iters && converged);
-    ctl->iter = it;
-    ctl->done = done ? 1u : 0u;
-    ctl->max_err_bits = 0;
-    ctl->blocks_done = 0;
-    if (ctl->fast_particles != ctl->fast_at_begin) ctl->list_fallbacks += 1;
-    if (done) close_step(ctl, it, rel, converged);
 }
 
 // pcisph.cl:65-92, and the neighbour list of the step. kBoundary: the scene has boundary particles (their
