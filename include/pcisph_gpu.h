@@ -259,7 +259,8 @@ PCISPH_API int pcisph_autotune(pcisph_ctx* ctx, uint32_t steps, pcisph_tune_resu
  * setters' values, the options, then the fluid positions and velocities (float4 per particle, sorted
  * order of the last step) and the boundary positions as set (float4). pcisph_snapshot synchronises the
  * context's stream. pcisph_restore sets the parameters and options, re-derives them and loads the state,
- * so the next update continues exactly where the snapshot was taken. No counterpart in the reference. */
+ * so the next update continues exactly where the snapshot was taken; the step counter of pcisph_last_stats
+ * continues from the snapshot's, the other statistics start over. No counterpart in the reference. */
 PCISPH_API int pcisph_snapshot_size(pcisph_ctx* ctx, size_t* bytes);
 PCISPH_API int pcisph_snapshot(pcisph_ctx* ctx, void* dst, size_t dst_bytes);
 PCISPH_API int pcisph_restore(pcisph_ctx* ctx, const void* src, size_t src_bytes);
