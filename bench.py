@@ -293,6 +293,12 @@ def _oracle_for(scene):
     return O, p, opts
 
 
+def oracle_threads():
+    """The OpenMP threads the oracle's loops ran on (the cores the CPU baseline used)."""
+    from oracle.oracle import get as get_oracle
+    return get_oracle().num_threads()
+
+
 def cpu_step_rate(scene, pos, vel, seconds, max_steps=None):
     """Oracle steps from (pos, vel) until `seconds` of step time; returns (particle-steps/s, steps, iters).
     Boundary particles are sorted in the first step only, as the GPU context sorts them once."""
@@ -354,6 +360,7 @@ def reference_arm(args, rank, world):
         _, _, _, s = cpu_step_rate(sc, pos, vel, float("inf"), max_steps=w)
         pos, vel = s["f_pos"], s["f_vel"]
     rate, steps, iters, _ = cpu_step_rate(sc, pos, vel, REFERENCE_TIMED_SECONDS, max_steps=args.steps)
+    cores = oracle_threads()
     line = {
         "impl": "reference", "metric": metric, "value": rate,
         "unit": "particle-steps/s", "n_gpus": world, "steps": steps, "warmup": w,
@@ -506,7 +513,7 @@ def scenes_workload(args, rank, world, local, emit=True, cpu_leg=True):
             done += sc[k].fluid_count * steps_k
             t_cpu += sc[k].fluid_count * steps_k / r
             cs += steps_k
-        cpu = {"value": done / t_cpu, "unit": "particle-steps/s", "cores": os.cpu_count(), "kind": "port",
+        cpu = {"value": done / t_cpu, "unit": "particle-steps/s", "cores": oracle_threads(), "kind": "port",
                "sample": f"the 8 smallest scenes, {cs} scene-steps from the timed loop's start state "
                          f"(oracle/pcisph_oracle.cpp with OpenMP)"}
     if rank == 0:
@@ -810,7 +817,7 @@ def main():
     cpu = None
     if rank == 0 and world == 1:
         rate, csteps, citers = cpu_sample_rate(sc, samples, args.cpu_seconds, max_steps=args.steps)
-        cpu = {"value": rate, "unit": "particle-steps/s", "cores": os.cpu_count(), "kind": "port",
+        cpu = {"value": rate, "unit": "particle-steps/s", "cores": oracle_threads(), "kind": "port",
                "sample": f"{N} particles x {csteps} steps, one step at a time from the states at {len(samples)} "
                          f"evenly spaced points of the timed steps (mean {citers:.2f} corrective iterations "
                          f"against the GPU's {iters:.2f}), oracle/pcisph_oracle.cpp with OpenMP",

@@ -88,6 +88,7 @@ class Oracle:
         L = self.lib
         assert L.or_sizeof_params() == 80 and L.or_sizeof_params() == C.sizeof(SimParams)
         assert L.or_sizeof_options() == C.sizeof(Options)
+        L.or_num_threads.restype = C.c_int
         L.or_derive_params.argtypes = [C.c_float, C.c_float, C.c_uint32, C.c_uint32, C.c_float, C.c_float,
                                        C.c_float, C.c_float, C.POINTER(SimParams)]
         L.or_sort_bit_count.argtypes = [C.c_uint32]
@@ -108,6 +109,10 @@ class Oracle:
         L.or_pressure_force.argtypes = [P, u32p, f32p, f32p, u32p, f32p, f32p, f32p, f32p]
         L.or_step_f32.argtypes = [P, C.POINTER(Options), C.POINTER(_StateF32), C.c_int, C.POINTER(Stats)]
         L.or_step_f64.argtypes = [P, C.POINTER(Options), C.POINTER(_StateF64), C.c_int, C.POINTER(Stats)]
+
+    def num_threads(self):
+        """OpenMP threads of the oracle's parallel loops."""
+        return self.lib.or_num_threads()
 
     # -- params -----------------------------------------------------------
     def derive_params(self, particle_radius, rest_density, fluid_count, boundary_count, delta_t, gravity,

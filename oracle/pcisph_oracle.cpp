@@ -53,6 +53,8 @@
 #include <climits>
 #include <vector>
 
+#include <omp.h>
+
 typedef uint32_t u32;
 
 /* Mirror of Simulation_Params (data/kernels/Simulation_Params.h:18-44): 20 x 4 B. */
@@ -485,6 +487,8 @@ static void pressure_force(const OrParams* p, const u32* b_off, const T* b_pos, 
 extern "C" {
 int or_sizeof_params(void) { return (int)sizeof(OrParams); }
 int or_sizeof_options(void) { return (int)sizeof(OrOptions); }
+// The OpenMP threads a parallel region of this library runs on (the CPU baseline reports them).
+int or_num_threads(void) { return omp_get_max_threads(); }
 void or_update_density(const OrParams* p, const u32* b_off, const float* b_pos, const u32* f_off, const float* f_pos,
                        float* rho) { density<float>(p, b_off, b_pos, f_off, f_pos, rho); }
 void or_update_normal(const OrParams* p, const u32* f_off, const float* f_pos, const float* rho, float* nrm) {
