@@ -51,7 +51,8 @@ class Options(C.Structure):
     _fields_ = [("min_iterations", C.c_int32), ("max_iterations", C.c_int32), ("walls", C.c_int32),
                 ("box_lo", C.c_float * 3), ("box_hi", C.c_float * 3), ("restitution", C.c_float),
                 ("boundary_self_density", C.c_int32), ("loop_mode", C.c_int32), ("kernel_variant", C.c_int32),
-                ("list_skin", C.c_float), ("spatial_order", C.c_int32), ("sweep_block", C.c_int32)]
+                ("list_skin", C.c_float), ("spatial_order", C.c_int32), ("sweep_block", C.c_int32),
+                ("particle_skin", C.c_int32)]
 
 
 class StepStats(C.Structure):

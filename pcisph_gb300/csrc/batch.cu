@@ -155,7 +155,7 @@ struct pcisph_batch {
     ListBuffers list_buffers() const {
         return ListBuffers{pos, vel, pr4, normal, f_other, f_press, pred, pf4, state_pos, state_vel, rho, press, err,
                            cells, cells, nullptr, nullptr, nbr, nbr_count, near, near_count, bucket_fast,
-                           n_particles, nullptr, nullptr, nullptr, nullptr};
+                           n_particles, /*out_index*/ nullptr, /*disp_max*/ nullptr, /*state_skin*/ nullptr};
     }
 
     uint32_t pool_end() const { return scenes.empty() ? 0u : scenes.back().offset + scenes.back().count; }

@@ -32,6 +32,12 @@ struct DevParams {
     uint32_t bfl_cap;   // entries of a boundary particle's fluid list (fluid particles within r_list)
     float near_r2;      // within-h list radius^2: h^2 (1 + 1e-4), a margin far above rounding
     float list_r, list_r2, list_half_skin;
+    // per-particle skins (one scene): particle i's lists take the radius h + sh_i + skin_max_half, sh_i its own
+    // half skin (twice its largest predicted displacement of the previous step, within [skin_min_half,
+    // skin_max_half]); a prediction past its own sh_i makes that particle walk, one past skin_max_half makes
+    // its neighbourhood walk (as with one skin). 0: every particle has skin_max_half (half the list skin).
+    int particle_skin;
+    float skin_min_half, skin_max_half, skin_factor;
     // batched scenes with an adaptive skin: each step picks one of kSkinLevels skins from the previous
     // step's count of predictions past each level's half skin (skin_half[k])
     int adaptive_skin;
@@ -93,6 +99,36 @@ __host__ __device__ inline void set_list_skin(DevParams* d, float skin) {
     d->list_r = d->h * (1.f + skin);
     d->list_r2 = d->list_r * d->list_r;
     d->list_half_skin = 0.5f * d->h * skin - 1e-6f * d->h;
+    d->skin_max_half = 0.5f * d->h * skin;
+}
+
+// Particle k's half skin from its stored value w (the largest, skin_max_half, without per-particle skins or
+// when w is 0, NaN or out of range).
+__host__ __device__ inline float half_skin_of(const DevParams& P, float w) {
+    return (P.particle_skin && w >= P.skin_min_half && w <= P.skin_max_half) ? w : P.skin_max_half;
+}
+
+// A prediction that moved farther than this from x is fast (its lists may miss a pair): half the skin less
+// a margin for the rounding of |x* - x| and |x_i - x_j| (1e-6 h, far above it).
+__host__ __device__ inline float fast_threshold(const DevParams& P, float half_skin) {
+    return half_skin - 1e-6f * P.h;
+}
+
+// The list radius^2 of particle i (half skin sh_i) for fluid candidates: a pair within h at the predictions
+// is within h + d_i + d_j at x, so h + sh_i + skin_max_half holds it while i moved at most sh_i and the
+// candidate at most skin_max_half (a candidate past it flags its bucket). Without per-particle skins: the
+// list radius h (1 + skin).
+__host__ __device__ inline float particle_list_r2(const DevParams& P, float sh_i) {
+    if (!P.particle_skin) return P.list_r2;
+    const float r = P.h + sh_i + P.skin_max_half;
+    return r * r;
+}
+
+// The same for a boundary candidate (boundary particles do not move).
+__host__ __device__ inline float boundary_list_r2(const DevParams& P, float sh_i) {
+    if (!P.particle_skin) return P.list_r2;
+    const float r = P.h + sh_i;
+    return r * r;
 }
 
 __host__ __device__ inline void magic_for(uint32_t d, uint32_t* magic, uint32_t* shift) {

@@ -54,7 +54,7 @@ int fail(int code, const std::string& msg) {
 
 size_t fluid_arena_bytes(uint32_t n, uint32_t bk) {
     return 10 * align256((size_t)n * 16) + 3 * align256((size_t)n * 4) + 4 * align256((size_t)n * 4) +
-           align256((size_t)bk * 8);
+           2 * align256((size_t)n * 4) + align256((size_t)bk * 8);
 }
 size_t boundary_arena_bytes(uint32_t n, uint32_t bk) {
     return 3 * align256((size_t)n * 16) + 5 * align256((size_t)n * 4) + align256((size_t)bk * 8);
@@ -120,7 +120,8 @@ struct pcisph_ctx {
         return ListBuffers{b.pos, b.vel, b.pr4, b.normal, b.f_other, b.f_press, b.pred, b.pf4, b.state_pos,
                            b.state_vel, b.rho, b.press, b.err, w ? cells_w : b.cells, b.b_cells, b.b_pos, b.bpf,
                            b.nbr, b.nbr_count, b.near, b.near_count, b.bucket_fast, P.fluid_count,
-                           w ? d_of_w : nullptr, b.b_init, b.b_press, b.b_near, b.bnbr, b.bnbr_count, b.bfl,
+                           w ? d_of_w : nullptr, b.disp_max, b.state_skin, b.b_init, b.b_press, b.b_near, b.bnbr,
+                           b.bnbr_count, b.bfl,
                            b.bfl_count, zone_map, {zone_org[0], zone_org[1], zone_org[2]},
                            {zone_dim[0], zone_dim[1], zone_dim[2]}};
     }
@@ -182,7 +183,7 @@ struct pcisph_ctx {
         timed("working_ranges", s, [&] { launch_working_ranges(order, BK, b.cells, cells_w, range_scratch, N, s); });
         timed("permute", s, [&] {
             launch_permute(sk, sv, b.state_pos, b.state_vel, N, BK, b.cells, cells_w, b.pos, b.vel, d_of_w, w_of_d,
-                           b.ctl, s);
+                           b.ctl, s, P.particle_skin ? b.state_skin : nullptr);
         });
         nl += 4;
         return cudaGetLastError() == cudaSuccess ? nl : -1;
@@ -286,6 +287,8 @@ struct pcisph_ctx {
         f_ids = c.take<uint32_t>(n);
         b.codes = c.take<uint32_t>(n);
         b.groups = c.take<uint32_t>(n);
+        b.state_skin = c.take<float>(n);  // zero: "no skin yet", read as the largest
+        b.disp_max = c.take<float>(n);
         b.cells = c.take<uint2>(bk);
         CUDA_TRY(cudaMemsetAsync(fluid_block.p, 0, fluid_arena_bytes(n, bk), stream()));
         fluid_cap_n = n;
@@ -338,6 +341,10 @@ struct pcisph_ctx {
     void build_devparams() {
         make_devparams(params, opts.min_iterations, opts.max_iterations, opts.walls, opts.box_lo, opts.box_hi,
                        opts.restitution, threshold, opts.list_skin, 0, &P);
+        const bool skins = opts.particle_skin == 1 || (opts.particle_skin == 2 && params.boundary_count > 0);
+        P.particle_skin = skins && list_sweeps() ? 1 : 0;
+        P.skin_min_half = std::min(kSkinMinHalf * P.h, P.skin_max_half);
+        P.skin_factor = kSkinFactor;
         graph_valid = false;
         order_age = kNoOrder;
     }
@@ -467,7 +474,10 @@ struct pcisph_ctx {
             if (r2 < 0) return -1;
             nl += r2 - 1;  // the reorder launch is counted below
         } else {
-            timed("reorder", s, [&] { launch_reorder(sk, sv, b.state_pos, b.state_vel, N, b.pos, b.vel, b.cells, b.codes, b.groups, P, b.ctl, s); });
+            timed("reorder", s, [&] {
+                launch_reorder(sk, sv, b.state_pos, b.state_vel, N, b.pos, b.vel, b.cells, b.codes, b.groups, P, b.ctl,
+                               s, P.particle_skin ? b.state_skin : nullptr);
+            });
         }
         const SweepArgs A = sweep_args();
         if (list_sweeps()) {
@@ -703,7 +713,8 @@ struct pcisph_ctx {
                     if (r2 < 0) return fail(PCISPH_ERR_CUDA, "working order of the sort stage failed");
                     host_launches += nl + 1 + r2;
                 } else {
-                    launch_reorder(sk, sv, b.state_pos, b.state_vel, N, b.pos, b.vel, b.cells, b.codes, b.groups, P, b.ctl, s);
+                    launch_reorder(sk, sv, b.state_pos, b.state_vel, N, b.pos, b.vel, b.cells, b.codes, b.groups, P,
+                                   b.ctl, s, P.particle_skin ? b.state_skin : nullptr);
                     host_launches += nl + 2;
                 }
                 break;
@@ -836,6 +847,14 @@ struct pcisph_ctx {
             CUDA_TRY(cudaGetLastError());
             v.ptr = xfer;
         }
+        if (field == PCISPH_FIELD_SORTED_POSITION && layout == PCISPH_LAYOUT_FLOAT4 && P.particle_skin) {
+            // w of the step's positions holds each particle's half skin: export 0 there
+            float4* tmp = v.ptr == xfer ? xfer : static_cast<float4*>(staging_block.p);
+            launch_xyz0(static_cast<const float4*>(v.ptr), tmp, (uint32_t)v.count, s);
+            ++host_launches;
+            CUDA_TRY(cudaGetLastError());
+            v.ptr = tmp;
+        }
         if (layout == PCISPH_LAYOUT_PACKED3) {
             void* pinned = memory == PCISPH_MEM_HOST ? host::pinned_device_view(dst) : nullptr;
             float* out = memory == PCISPH_MEM_HOST ? static_cast<float*>(pinned ? pinned : staging_block.p)
@@ -967,6 +986,7 @@ int pcisph_default_options(pcisph_options* o) {
     o->list_skin = 0.25f;
     o->spatial_order = 2;
     o->sweep_block = 256;
+    o->particle_skin = 2;
     return PCISPH_OK;
 }
 
@@ -1050,6 +1070,7 @@ int pcisph_set_options(pcisph_ctx* ctx, const pcisph_options* o) {
         return fail(PCISPH_ERR_INVALID_ARG, "list_skin must be in [0, 2]");
     if (o->sweep_block != 128 && o->sweep_block != 256 && o->sweep_block != 512)
         return fail(PCISPH_ERR_INVALID_ARG, "sweep_block must be 128, 256 or 512");
+    if (o->particle_skin < 0 || o->particle_skin > 2) return fail(PCISPH_ERR_INVALID_ARG, "particle_skin must be 0, 1 or 2");
     const bool bsd_changed = o->boundary_self_density != ctx->opts.boundary_self_density;
     ctx->opts = *o;
     if (bsd_changed) ctx->boundary_updated = true;
@@ -1224,6 +1245,16 @@ int pcisph_field_device_ptr(pcisph_ctx* ctx, int field, void** ptr, size_t* coun
         if (e.ensure(v.count * esz) != cudaSuccess) return fail(PCISPH_ERR_OOM, "device allocation of a field copy failed");
         if (esz == 16) launch_gather4(static_cast<const float4*>(v.ptr), ctx->w_of_d, static_cast<float4*>(e.p), (uint32_t)v.count, ctx->stream());
         else launch_gather1(static_cast<const float*>(v.ptr), ctx->w_of_d, static_cast<float*>(e.p), (uint32_t)v.count, ctx->stream());
+        ++ctx->host_launches;
+        CUDA_TRY(cudaGetLastError());
+        v.ptr = e.p;
+    }
+    if (field == PCISPH_FIELD_SORTED_POSITION && ctx->P.particle_skin && v.ptr && v.count) {
+        // w of the step's positions holds each particle's half skin: hand out a copy with 0 there
+        DeviceGuard g(ctx->device);
+        DeviceBlock& e = ctx->exports[field];
+        if (e.ensure(v.count * 16) != cudaSuccess) return fail(PCISPH_ERR_OOM, "device allocation of a field copy failed");
+        launch_xyz0(static_cast<const float4*>(v.ptr), static_cast<float4*>(e.p), (uint32_t)v.count, ctx->stream());
         ++ctx->host_launches;
         CUDA_TRY(cudaGetLastError());
         v.ptr = e.p;

@@ -40,6 +40,10 @@ inline constexpr uint32_t kListCapWide = 168;
 // adaptive skin: a level qualifies if at most 1 in this many of the last step's predictions outran it
 // (256 batched scenes, 9.8M particles, 500 steps: 27.1, 27.0, 27.1, 27.3 s at 500, 3000, 20000, 10^6)
 inline constexpr uint32_t kSkinOutrunRatio = 500;
+// per-particle skins: a particle's next half skin is kSkinFactor times its largest predicted displacement of
+// the step, at least kSkinMinHalf h (measured at 1M: 0.00-0.05% of the predictions then outrun their skin)
+inline constexpr float kSkinFactor = 2.0f;
+inline constexpr float kSkinMinHalf = 0.02f;
 
 // Wait up to timeout_ms for the work queued on s (0: look once). *done = false when it is still running at
 // the deadline; the work is left queued and a later wait can pick it up.

@@ -224,12 +224,15 @@ __global__ void __launch_bounds__(kBlock) k_boundary_pressure_list(DevParams P, 
 // pcisph.cl:65-92, and the neighbour list of the step. kBoundary: the scene has boundary particles (their
 // walk and list are compiled out otherwise: the fluid-only builder measured 5% slower with them present)
 template <class PS, bool kBoundary>
-__global__ void __launch_bounds__(kBlock) k_density_list(PS ps, ListBuffers b) {
+// (at most 40 registers: 6 blocks, 48 warps per SM; 46 registers measured 5% slower at 1M)
+__global__ void __launch_bounds__(kBlock, 6) k_density_list(PS ps, ListBuffers b) {
     const uint32_t i = blockIdx.x * kBlock + threadIdx.x;
     if (i >= ps.count()) return;
     const DevParams& P = ps.params(i);
-    const float4 xi = b.pos[i];
+    const float4 xi = b.pos[i];  // xi.w: the particle's stored half skin
     const Cell c = cell_of(xi.x, xi.y, xi.z, P);
+    const float sh_i = half_skin_of(P, xi.w);
+    const float list_r2 = particle_list_r2(P, sh_i), blist_r2 = boundary_list_r2(P, sh_i);
     float acc = 0.f;
     const uint32_t stride = b.nbr_stride;
     // current chunk of each thread's skin and within-h lists; the boundary list's chunks go through the
@@ -249,7 +252,7 @@ __global__ void __launch_bounds__(kBlock) k_density_list(PS ps, ListBuffers b) {
             const float4 o = __ldg(&b.b_pos[j]);
             const float r2 = dist2(xi.x - o.x, xi.y - o.y, xi.z - o.z);
             acc += poly6(r2, P.h2);  // density_term's expression
-            if (r2 <= P.list_r2) {
+            if (r2 <= blist_r2) {
                 if (b.bnbr && nb < P.bnd_cap) list_append(b.bnbr, i, stride, bbuf, nb, j);
                 ++nb;
             }
@@ -266,7 +269,7 @@ __global__ void __launch_bounds__(kBlock) k_density_list(PS ps, ListBuffers b) {
         const float dx = xi.x - o.x, dy = xi.y - o.y, dz = xi.z - o.z;
         const float r2 = dist2(dx, dy, dz);
         acc += poly6(r2, P.h2);
-        if (r2 <= P.list_r2) {
+        if (r2 <= list_r2) {
             if (n < P.list_cap) list_append(b.nbr, i, stride, fbuf, n, j);
             ++n;
             if (r2 <= P.near_r2) {
@@ -326,7 +329,8 @@ __global__ void __launch_bounds__(kBlock) k_force_list(PS ps, ListBuffers b) {
     const float3 dx = v * P.dt;
     const float4 xs = make_float4(xi.x + dx.x, xi.y + dx.y, xi.z + dx.z, 0.f);
     b.pred[i] = xs;
-    note_displacement(P, ps.control(i), b.bucket_fast, xi, xs);
+    const float disp = note_displacement(P, ps.control(i), b.bucket_fast, xi, xs, P.list_half_skin);
+    if (P.particle_skin) b.disp_max[i] = disp;
 }
 
 // pcisph.cl:212-263 (boundary_update = 0); one scene: also the stop decision in the last block
@@ -344,14 +348,20 @@ __device__ __forceinline__ float pressure_body(const PS& ps, const ListBuffers& 
         float acc = 0.f;
         const uint32_t cnt = b.nbr_count[i];
         const bool overflow = cnt > P.list_cap;
-        // boundary terms: all zero unless a boundary particle was within r_list of x, or x* moved more than
-        // half the skin from x (boundary particles do not move). Within half the skin, the boundary list
-        // (every boundary particle within r_list of x) holds every one that can be within h of x*.
+        // self_fast: x* moved more than the particle's own half skin from x, so its lists (built for that
+        // skin) may miss a pair: with per-particle skins it walks. Boundary terms: all zero unless a boundary
+        // particle was within r_list of x, or x* moved past the half skin (boundary particles do not move);
+        // within it, the boundary list (every boundary particle within r_list of x) holds every one that can
+        // be within h of x*.
+        bool self_fast = false;
+        if (P.particle_skin || P.boundary_count) {
+            const float dx = xp.x - xi.x, dy = xp.y - xi.y, dz = xp.z - xi.z;
+            self_fast = sqrtf(dist2(dx, dy, dz)) > fast_threshold(P, half_skin_of(P, xi.w));
+        }
         bool walk_boundary = false, list_boundary = false;
         uint32_t bcnt = 0;
         if (P.boundary_count) {
-            const float dx = xp.x - xi.x, dy = xp.y - xi.y, dz = xp.z - xi.z;
-            if (sqrtf(dist2(dx, dy, dz)) > P.list_half_skin) {
+            if (self_fast) {
                 walk_boundary = true;
             } else if (b.b_near[i] != 0) {
                 if (b.bnbr) bcnt = b.bnbr_count[i];
@@ -360,8 +370,9 @@ __device__ __forceinline__ float pressure_body(const PS& ps, const ListBuffers& 
             }
         }
         Cell c{0u, 0u, 0u};  // the cell (three IEEE divisions) only where a walk may need it
-        if (overflow || !all_lists_ok || walk_boundary) c = cell_of(xi.x, xi.y, xi.z, P);
-        const bool walk = overflow || (!all_lists_ok && near_fast(P, b.bucket_fast, c));
+        const bool own_walk = overflow || (P.particle_skin && self_fast);
+        if (own_walk || !all_lists_ok || walk_boundary) c = cell_of(xi.x, xi.y, xi.z, P);
+        const bool walk = own_walk || (!all_lists_ok && near_fast(P, b.bucket_fast, c));
         auto fb = [&](uint32_t j) { acc += density_term(xp.x, xp.y, xp.z, __ldg(&b.b_pos[j]), P.h2); };
         if (walk_boundary) for_each_neighbour(b.b_cells, c, P, fb);
         else if (list_boundary) for_each_listed(b.bnbr, i, bcnt, b.nbr_stride, fb);
@@ -461,7 +472,8 @@ __device__ __forceinline__ void pressure_force_body(const PS& ps, const ListBuff
     if (!integrate) {
         const float4 xs = f4(x, 0.f);
         b.pred[i] = xs;
-        note_displacement(P, ctl, b.bucket_fast, xi, xs);
+        const float disp = note_displacement(P, ctl, b.bucket_fast, xi, xs, P.list_half_skin);
+        if (P.particle_skin) b.disp_max[i] = fmaxf(b.disp_max[i], disp);
         return;
     }
     if (P.walls) {
@@ -481,6 +493,8 @@ __device__ __forceinline__ void pressure_force_body(const PS& ps, const ListBuff
     const uint32_t o = b.out_index ? b.out_index[i] : i;  // working order -> sorted order
     b.state_pos[o] = f4(x, 0.f);
     b.state_vel[o] = f4(v, 0.f);
+    if (P.particle_skin)  // the next step's half skin: twice this step's largest predicted displacement
+        b.state_skin[o] = fminf(fmaxf(P.skin_factor * b.disp_max[i], P.skin_min_half), P.skin_max_half);
 }
 
 template <class PS, int BS = kBlock>

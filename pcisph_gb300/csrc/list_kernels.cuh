@@ -23,6 +23,8 @@ struct ListBuffers {
     unsigned char* bucket_fast;  // per bucket of the cell table: holds a fast particle this step
     uint32_t nbr_stride;         // particles in the arrays (>= every index i)
     const uint32_t* out_index;   // integration writes particle i's state at out_index[i] (null: at i)
+    float* disp_max;             // per-particle skins: particle i's largest predicted displacement this step
+    float* state_skin;           // per-particle skins: the next step's half skin, stored beside the state
     const float* b_init;         // boundary initial (self) densities and pressures (single scene, B > 0)
     float* b_press;
     unsigned char* b_near;       // per fluid particle (B > 0): a boundary particle within r_list of x at the

@@ -128,7 +128,7 @@ __global__ void __launch_bounds__(kBlock) k_permute(const uint32_t* __restrict__
                                                     const uint2* __restrict__ cells_d, const uint2* __restrict__ cells_w,
                                                     float4* __restrict__ pos_w, float4* __restrict__ vel_w,
                                                     uint32_t* __restrict__ d_of_w, uint32_t* __restrict__ w_of_d,
-                                                    Control* ctl) {
+                                                    Control* ctl, const float* __restrict__ state_skin) {
     const uint32_t d = blockIdx.x * kBlock + threadIdx.x;
     if (d >= n) return;
     const uint32_t key = sk[d], src = sv[d];
@@ -139,7 +139,9 @@ __global__ void __launch_bounds__(kBlock) k_permute(const uint32_t* __restrict__
         atomicOr(&ctl->status, 4u);
         return;
     }
-    pos_w[w] = state_pos[src];
+    float4 p = state_pos[src];
+    if (state_skin) p.w = state_skin[src];  // the particle's stored half skin rides in w
+    pos_w[w] = p;
     vel_w[w] = state_vel[src];
     d_of_w[w] = d;
     w_of_d[d] = w;
@@ -177,6 +179,14 @@ __global__ void __launch_bounds__(kBlock) k_scatter1(const float* __restrict__ s
         if (j < n) dst[j] = src[i];
     }
 }
+// out[i] = (in[i].xyz, 0); in place when out == in
+__global__ void __launch_bounds__(kBlock) k_xyz0(const float4* in, float4* out, uint32_t n) {
+    const uint32_t i = blockIdx.x * kBlock + threadIdx.x;
+    if (i < n) {
+        const float4 v = in[i];
+        out[i] = make_float4(v.x, v.y, v.z, 0.f);
+    }
+}
 __global__ void __launch_bounds__(kBlock) k_iota(uint32_t* a, uint32_t n) {
     const uint32_t i = blockIdx.x * kBlock + threadIdx.x;
     if (i < n) a[i] = i;
@@ -203,10 +213,11 @@ void launch_working_ranges(const uint32_t* order, uint32_t bk, const uint2* cell
 
 void launch_permute(const uint32_t* sorted_keys, const uint32_t* sorted_ids, const float4* state_pos,
                     const float4* state_vel, uint32_t n, uint32_t bk, const uint2* cells_d, const uint2* cells_w,
-                    float4* pos_w, float4* vel_w, uint32_t* d_of_w, uint32_t* w_of_d, Control* ctl, cudaStream_t s) {
+                    float4* pos_w, float4* vel_w, uint32_t* d_of_w, uint32_t* w_of_d, Control* ctl, cudaStream_t s,
+                    const float* state_skin) {
     if (n)
         k_permute<<<grid_for(n), kBlock, 0, s>>>(sorted_keys, sorted_ids, state_pos, state_vel, n, bk, cells_d, cells_w,
-                                                 pos_w, vel_w, d_of_w, w_of_d, ctl);
+                                                 pos_w, vel_w, d_of_w, w_of_d, ctl, state_skin);
 }
 
 void launch_gather4(const float4* src, const uint32_t* idx, float4* dst, uint32_t n, cudaStream_t s) {
@@ -220,6 +231,9 @@ void launch_scatter4(const float4* src, const uint32_t* idx, float4* dst, uint32
 }
 void launch_scatter1(const float* src, const uint32_t* idx, float* dst, uint32_t n, cudaStream_t s) {
     if (n) k_scatter1<<<grid_for(n), kBlock, 0, s>>>(src, idx, dst, n);
+}
+void launch_xyz0(const float4* in, float4* out, uint32_t n, cudaStream_t s) {
+    if (n) k_xyz0<<<grid_for(n), kBlock, 0, s>>>(in, out, n);
 }
 void launch_iota(uint32_t* a, uint32_t n, cudaStream_t s) {
     if (n) k_iota<<<grid_for(n), kBlock, 0, s>>>(a, n);

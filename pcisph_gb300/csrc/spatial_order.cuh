@@ -32,13 +32,16 @@ void launch_working_ranges(const uint32_t* order, uint32_t bk, const uint2* cell
 // pos_w/vel_w[w] = state[sorted_ids[d]] for sorted index d at working index w; d_of_w and w_of_d.
 void launch_permute(const uint32_t* sorted_keys, const uint32_t* sorted_ids, const float4* state_pos,
                     const float4* state_vel, uint32_t n, uint32_t bk, const uint2* cells_d, const uint2* cells_w,
-                    float4* pos_w, float4* vel_w, uint32_t* d_of_w, uint32_t* w_of_d, Control* ctl, cudaStream_t s);
+                    float4* pos_w, float4* vel_w, uint32_t* d_of_w, uint32_t* w_of_d, Control* ctl, cudaStream_t s,
+                    const float* state_skin = nullptr);
 
 // dst[i] = src[idx[i]] and dst[idx[i]] = src[i] for float4 and float elements; iota: a[i] = i.
 void launch_gather4(const float4* src, const uint32_t* idx, float4* dst, uint32_t n, cudaStream_t s);
 void launch_gather1(const float* src, const uint32_t* idx, float* dst, uint32_t n, cudaStream_t s);
 void launch_scatter4(const float4* src, const uint32_t* idx, float4* dst, uint32_t n, cudaStream_t s);
 void launch_scatter1(const float* src, const uint32_t* idx, float* dst, uint32_t n, cudaStream_t s);
+// out = (in.xyz, 0) (in place when out == in): the step's positions without the per-particle skin in w.
+void launch_xyz0(const float4* in, float4* out, uint32_t n, cudaStream_t s);
 void launch_iota(uint32_t* a, uint32_t n, cudaStream_t s);
 
 }  // namespace pcisph

@@ -51,7 +51,8 @@ __global__ void __launch_bounds__(kBlock) k_reorder(const uint32_t* __restrict__
                                                     const float4* __restrict__ in_vel, uint32_t n,
                                                     float4* __restrict__ out_pos, float4* __restrict__ out_vel,
                                                     uint2* __restrict__ cells, uint32_t* __restrict__ codes,
-                                                    uint32_t* __restrict__ groups, DevParams P, Control* ctl) {
+                                                    uint32_t* __restrict__ groups, DevParams P, Control* ctl,
+                                                    const float* __restrict__ in_skin) {
     const uint32_t d = blockIdx.x * kBlock + threadIdx.x;
     if (d >= n) return;
     const uint32_t src = ids[d];
@@ -59,7 +60,8 @@ __global__ void __launch_bounds__(kBlock) k_reorder(const uint32_t* __restrict__
     const bool ok = src < n && key < P.bucket_count;
     bool is_start = false;
     if (ok) {
-        const float4 p = in_pos[src];
+        float4 p = in_pos[src];
+        if (in_skin) p.w = in_skin[src];  // the particle's stored half skin rides in w
         out_pos[d] = p;
         if (in_vel) out_vel[d] = in_vel[src];
         if (codes) {
@@ -394,10 +396,10 @@ void launch_hash(const float* pos, bool packed, uint32_t n, const DevParams& P, 
 
 void launch_reorder(const uint32_t* keys, const uint32_t* ids, const float4* in_pos, const float4* in_vel,
                     uint32_t n, float4* out_pos, float4* out_vel, uint2* cells, uint32_t* codes, uint32_t* groups,
-                    const DevParams& P, Control* ctl, cudaStream_t s) {
+                    const DevParams& P, Control* ctl, cudaStream_t s, const float* in_skin) {
     if (!n) return;
     k_reorder<<<grid_for(n), kBlock, 0, s>>>(keys, ids, in_pos, in_vel, n, out_pos, out_vel, cells, codes, groups, P,
-                                             ctl);
+                                             ctl, in_skin);
 }
 
 void launch_begin(Control* ctl, cudaStream_t s) { k_begin<<<1, 1, 0, s>>>(ctl); }

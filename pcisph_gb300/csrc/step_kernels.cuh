@@ -24,6 +24,8 @@ struct StepBuffers {
     uint2* cells;                    // fluid cell table [bucket_count]
     uint32_t* codes;                 // packed cell of each sorted particle (sweep.cuh cell_code)
     uint32_t* groups;                // start of every bucket run (count in ctl->n_groups)
+    float* state_skin;               // per-particle skins: each particle's half skin, in the state's order
+    float* disp_max;                 // per-particle skins: this step's largest predicted displacement
     uint32_t* nbr;                   // neighbour lists, list_cap entries per particle (kernel_variant 2)
     uint32_t* nbr_count;             // entries per particle; > list_cap means "walk the buckets"
     uint32_t* near;                  // within-h lists, near_cap entries per particle
@@ -48,7 +50,7 @@ void launch_hash(const float* pos, bool packed, uint32_t n, const DevParams& P, 
 // Also writes cell codes (if codes) and appends bucket-run starts to groups (if groups).
 void launch_reorder(const uint32_t* keys, const uint32_t* ids, const float4* in_pos, const float4* in_vel,
                     uint32_t n, float4* out_pos, float4* out_vel, uint2* cells, uint32_t* codes, uint32_t* groups,
-                    const DevParams& P, Control* ctl, cudaStream_t s);
+                    const DevParams& P, Control* ctl, cudaStream_t s, const float* in_skin = nullptr);
 void launch_begin(Control* ctl, cudaStream_t s);
 void launch_density(const DevParams& P, const StepBuffers& b, cudaStream_t s);
 void launch_normal(const DevParams& P, const StepBuffers& b, cudaStream_t s);

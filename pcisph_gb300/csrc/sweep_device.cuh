@@ -29,12 +29,13 @@ __device__ __forceinline__ void warp_count(unsigned long long* addr, bool pred) 
 // and is counted (one atomic per warp that has one; no store otherwise: in a splash most predictions are
 // fast, and a flag stored by each of their warps measured slower than the counts alone); the predictions
 // past each adaptive skin level are counted.
-__device__ __forceinline__ void note_displacement(const DevParams& P, Control* ctl,
-                                                  unsigned char* __restrict__ bucket_fast, const float4& xi,
-                                                  const float4& xs) {
+// Returns the displacement |x* - x|; threshold: the particle's fast_threshold.
+__device__ __forceinline__ float note_displacement(const DevParams& P, Control* ctl,
+                                                   unsigned char* __restrict__ bucket_fast, const float4& xi,
+                                                   const float4& xs, float threshold) {
     const float dx = xs.x - xi.x, dy = xs.y - xi.y, dz = xs.z - xi.z;  // exact: xs and xi are close
     const float disp = sqrtf(dist2(dx, dy, dz));
-    const bool fast = disp > P.list_half_skin;
+    const bool fast = disp > threshold;
     warp_count(&ctl->fast_particles, fast);
     if (P.adaptive_skin) {
 #pragma unroll
@@ -44,6 +45,7 @@ __device__ __forceinline__ void note_displacement(const DevParams& P, Control* c
         const Cell c = cell_of(xi.x, xi.y, xi.z, P);
         bucket_fast[P.bucket_base + hash_key(c.x, c.y, c.z, P)] = 1;
     }
+    return disp;
 }
 
 // The loop decision of one scene after its pressure sweep (Fluid.cpp:284-306).

@@ -682,6 +682,40 @@ def test_boundary_lists_change_no_bits(oracle, loop_mode, b_spacing, f_spacing):
             np.testing.assert_array_equal(out[skin][n], w, err_msg=f"skin {skin}: {n}")
 
 
+@pytest.mark.parametrize("loop_mode,order", [(0, 1), (2, 1), (0, 0)])
+def test_particle_skins_change_no_bits(oracle, loop_mode, order):
+    """Per-particle skins (the default with boundary particles: particle i's fluid list takes the radius
+    h + s_i + list_skin h / 2 and its boundary list h + s_i, s_i twice its largest predicted displacement of the
+    previous step within [0.02 h, list_skin h / 2]) give the same bits as one skin for every particle, over
+    steps in which the skins differ from particle to particle: a fluid block in a boundary box with some
+    particles thrown at the walls (a prediction past its own skin makes that particle walk), the persistent
+    loop and both particle orders included."""
+    d = 0.02
+    pos = scenes.lattice_block(10, 12, 10, d, (2 * d, 0.0, 2 * d), seed=23)
+    b_pos = scenes.boundary_box((0.0, 0.0, 0.0), (14 * d, 20 * d, 14 * d), d)
+    rng = np.random.default_rng(23)
+    vel = (rng.standard_normal(pos.shape) * 0.05).astype(np.float32)
+    fast = rng.choice(pos.shape[0], 30, replace=False)
+    vel[fast] = (rng.standard_normal((30, 3)) * 3.0).astype(np.float32)
+    p = oracle.derive_params(0.5 * d, 1000.0, pos.shape[0], b_pos.shape[0], 1e-3, -9.81, 0.2 * d ** 3, 0.5)
+    out = {}
+    for skins in (0, 1):
+        f = fluid_like(p, min_iters=3, max_iters=12, kernel_variant=2, loop_mode=loop_mode, spatial_order=order)
+        f.set_options(particle_skin=skins)
+        f.set_fluid_state(pos, vel)
+        f.set_boundary_state(b_pos)
+        f.step(6)
+        st = f.stats()
+        out[skins] = ({n: f.get_field(n) for n in ("position", "velocity", "density", "pressure", "pressure_force",
+                                                   "boundary_pressure", "sorted_position")},
+                      st.total_iterations, st.fast_particles)
+        f.close()
+    for n, w in out[0][0].items():
+        np.testing.assert_array_equal(out[1][0][n], w, err_msg=n)
+    assert out[1][1] == out[0][1]
+    assert out[1][2] >= out[0][2]  # smaller skins: as many or more predictions outrun theirs (those walk)
+
+
 def test_boundary_zone_changes_no_bits(oracle):
     """Fluid particles more than two cells from every boundary particle skip the builder's boundary walk
     (the boundary zone, a byte map over the boundary's cell box). One extra boundary particle 1 km away
