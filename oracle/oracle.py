@@ -109,6 +109,7 @@ class Oracle:
         L.or_pressure_force.argtypes = [P, u32p, f32p, f32p, u32p, f32p, f32p, f32p, f32p]
         L.or_step_f32.argtypes = [P, C.POINTER(Options), C.POINTER(_StateF32), C.c_int, C.POINTER(Stats)]
         L.or_step_f64.argtypes = [P, C.POINTER(Options), C.POINTER(_StateF64), C.c_int, C.POINTER(Stats)]
+        L.or_force_init_f64.argtypes = [P, u32p, f64p, f64p, f64p, f64p, f64p, f64p, f64p]
 
     def num_threads(self):
         """OpenMP threads of the oracle's parallel loops."""
@@ -173,6 +174,16 @@ class Oracle:
         N = p.fluid_count
         fo, pr, fp = np.empty((N, 3), np.float32), np.empty(N, np.float32), np.empty((N, 3), np.float32)
         self.lib.or_force_init(C.byref(p), _u(f_off), _f(pos), _f(nrm), _f(rho), _f(vel), _f(fo), _f(pr), _f(fp))
+        return fo, pr, fp
+
+    def force_init_f64(self, p, f_off, pos, nrm, rho, vel):
+        """force_init in FP64 on the same inputs (converted exactly from FP32)."""
+        N = p.fluid_count
+        d = lambda a: np.ascontiguousarray(a, np.float64)  # noqa: E731
+        pos, nrm, rho, vel = d(pos), d(nrm), d(rho), d(vel)
+        fo, pr, fp = np.empty((N, 3)), np.empty(N), np.empty((N, 3))
+        self.lib.or_force_init_f64(C.byref(p), _u(f_off), _ptr(pos, f64p), _ptr(nrm, f64p), _ptr(rho, f64p),
+                                   _ptr(vel, f64p), _ptr(fo, f64p), _ptr(pr, f64p), _ptr(fp, f64p))
         return fo, pr, fp
 
     def advance(self, p, pos, vel, f_other, f_press, integrate, options=None):

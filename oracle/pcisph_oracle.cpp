@@ -614,4 +614,9 @@ int or_step_f32(const OrParams* p, const OrOptions* o, OrState<float>* s, int bo
 int or_step_f64(const OrParams* p, const OrOptions* o, OrState<double>* s, int boundary_sort, OrStats* st) {
     return step<double>(p, o, s, boundary_sort, st);
 }
+// pcisph.cl:121-173 in FP64 on the given (FP32-valued) inputs: the rerun that settles pairs at r = h
+void or_force_init_f64(const OrParams* p, const u32* f_off, const double* pos, const double* nrm, const double* rho,
+                       const double* vel, double* f_other, double* press, double* f_press) {
+    force_init<double>(p, f_off, pos, nrm, rho, vel, f_other, press, f_press);
+}
 }

@@ -139,7 +139,9 @@ def test_dam_break_1m_warmed_step(oracle):
     f.close()
 
 
-def test_two_blocks_8m_sort_and_density(oracle):
+def test_two_blocks_8m_sort_and_sweeps(oracle):
+    """The 8M scene's sort (22-bit keys, three 8-bit passes) bit-exact, and its density, normal and force
+    sweeps (with the first predict) each against the oracle's kernel on the same inputs."""
     sc = scenes.two_blocks_8m()
     p, _ = _oracle_params(oracle, sc)
     assert p.bucket_count == 4194304 and oracle.sort_bit_count(p.bucket_count) == 22
@@ -156,9 +158,60 @@ def test_two_blocks_8m_sort_and_density(oracle):
     f.run_stage("density")
     rho = oracle.update_density(p, np.zeros(2 * p.bucket_count, np.uint32), np.zeros((0, 3), np.float32), off,
                                 spos)
-    e = rel_err(f.get_field("density"), rho)
-    print(f"8M density: {e:.1e}")
-    assert e <= RTOL
+    rho_g = f.get_field("density")
+    errs = {"density": rel_err(rho_g, rho)}
+    f.run_stage("normal")
+    nrm_g = f.get_field("normal")
+    errs["normal"] = rel_err(nrm_g, oracle.update_normal(p, off, spos, rho_g))
+    f.run_stage("force")
+    vel_g = f.get_field("sorted_velocity")
+    fo_g = f.get_field("other_force")
+    fo, _, _ = oracle.force_init(p, off, spos, nrm_g, rho_g, vel_g)
+    errs["other_force"] = rel_err(fo_g, fo)
+    report = {k: f"{v:.1e}" for k, v in errs.items()}
+    ok = {k: v <= RTOL for k, v in errs.items()}
+    if not ok["other_force"]:
+        # pairs at r = h (the 8M lattice has millions near 2d = h): settle against the FP64 rerun of the
+        # same kernel on the same inputs, as the step tests do
+        fo64, _, _ = oracle.force_init_f64(p, off, spos, nrm_g, rho_g, vel_g)
+        e64, own = rel_err(fo_g, fo64), rel_err(fo, fo64)
+        report["other_force"] += f" (vs FP64 {e64:.1e}, FP32 oracle vs FP64 {own:.1e})"
+        ok["other_force"] = e64 <= max(RTOL, 3 * own)
+    print("8M sweeps:", report)
+    assert all(ok.values()), report
+    f.close()
+
+
+def test_boundary_1m_warmed_step(oracle):
+    """The 1M dam break against 284,192 boundary particles (the boundary workload: the reference's 3-7
+    iterations, per-particle skins on), one step from the state after three warm-up steps: fluid and boundary
+    keys, permutations and cell ranges bit-exact, equal iterations, every field within the bound above, the
+    boundary pressures too."""
+    sc = scenes.dam_break_1m_boundary()
+    B = sc.boundary_count
+    f = _fluid(sc)
+    f.step(3)
+    pos, vel = f.get_field("position"), f.get_field("velocity")
+    f.update()
+    p = oracle.derive_params(sc.particle_radius, sc.rest_density, sc.fluid_count, B, sc.delta_t, sc.gravity,
+                             sc.viscosity_constant(), sc.surface_tension)
+    opts = make_options(threshold=sc.threshold, min_iters=sc.min_iters, max_iters=sc.max_iters, walls=sc.walls,
+                        box_lo=sc.box_lo, box_hi=sc.box_hi, restitution=sc.restitution)
+    s32 = oracle.new_state(p, pos, vel, sc.boundary_pos)
+    st32 = oracle.step(p, opts, s32, boundary_sort=True)
+    s64 = oracle.new_state(p, pos, vel, sc.boundary_pos, dtype=np.float64)
+    st64 = oracle.step(p, opts, s64, boundary_sort=True)
+    eq = np.testing.assert_array_equal
+    eq(f.get_field("boundary_keys"), s32["b_keys"])
+    eq(f.get_field("boundary_src"), s32["b_src"])
+    eq(f.get_field("boundary_cell_offsets"), s32["b_off"])
+    _compare_step("1M + boundary step 4", _ctx_getter(f), f.stats(), p, s32, st32, s64, st64)
+    scale = p.density_variation_scaling_factor * p.rest_density * st32.iterations
+    e = rel_err(f.get_field("boundary_pressure"), s32["b_press"], scale)
+    print(f"boundary pressure: {e:.1e}")
+    if e > RTOL:  # as for the fluid fields: no farther from FP64 than 3x the FP32 oracle
+        e64 = rel_err(f.get_field("boundary_pressure"), s64["b_press"], scale)
+        assert st64.iterations == st32.iterations and e64 <= max(RTOL, 3 * rel_err(s32["b_press"], s64["b_press"], scale))
     f.close()
 
 
@@ -191,3 +244,78 @@ def test_batched_scene_shapes_vs_oracle(oracle):
         assert (a.iterations, a.steps, a.total_iterations) == (b.iterations, b.steps, b.total_iterations)
         f.close()
     bt.close()
+
+
+def _ulp_nudged(pos, seed):
+    """pos with every coordinate moved by one ulp up or down (seeded signs): a perturbation of the size of the
+    rounding differences between two FP32 implementations of the same step, on every particle."""
+    sign = np.random.default_rng(seed).integers(0, 2, pos.shape).astype(bool)
+    pos = np.asarray(pos, np.float32)
+    return np.where(sign, np.nextafter(pos, np.float32(np.inf)), np.nextafter(pos, np.float32(-np.inf)))
+
+
+def test_dam_break_32k_long_run_statistics(oracle):
+    """The 32,768-particle dam break over its 1000 steps, GPU run against the oracle, in ten segments of 100
+    steps. SPH trajectories are chaotic (two runs part at the level of single particles within ~100 steps), so
+    at the start of each segment the oracle takes the GPU run's state, and over the segment the GPU's kinetic
+    energy (every 10 steps) and centre of mass must stay within 3x the larger drift of two oracle runs from
+    that state with every coordinate moved by one ulp (seeded signs: the size of the rounding differences
+    between two FP32 implementations), plus floors of 1e-3 of the run's largest kinetic energy and 1e-5 m.
+    Over the whole run: mean corrective iterations within 0.5, and the density-error gate: every step of the
+    GPU run that ends above the 1% threshold ends there in the oracle too, stepped from the GPU's state before
+    it (equal iterations, the same error within 1e-5 of rest density), and at most 0.5% of the steps of either
+    run end above it."""
+    from gpu_util import kinetic_energy
+    sc = scenes.dam_break_32k()
+    p, opts = _oracle_params(oracle, sc)
+    f = _fluid(sc)
+    iters_g, iters_o, above_g, above_o = [], [], 0, 0
+    ke_max = 0.0
+    worst = {"ke": 0.0, "com": 0.0}
+    for seg in range(10):
+        pos, vel = (sc.fluid_pos, np.zeros_like(sc.fluid_pos)) if seg == 0 else (f.get_field("position"),
+                                                                                f.get_field("velocity"))
+        runs = {"o": oracle.new_state(p, pos, vel)}
+        for r in range(2):
+            runs[f"b{r}"] = oracle.new_state(p, _ulp_nudged(pos, 100 * seg + r), vel)
+        ke = {key: [] for key in list(runs) + ["g"]}
+        com = {key: [] for key in ke}
+        for k in range(100):
+            prev = (f.get_field("position"), f.get_field("velocity"))
+            f.update()
+            st = f.stats()
+            iters_g.append(st.iterations)
+            if st.max_density_error >= sc.threshold:
+                above_g += 1
+                s2 = oracle.new_state(p, *prev)
+                so = oracle.step(p, opts, s2)
+                assert so.iterations == st.iterations, (seg * 100 + k + 1, so.iterations, st.iterations)
+                assert abs(so.max_err / p.rest_density - st.max_density_error) <= 1e-5, (seg * 100 + k + 1)
+            for key, s in runs.items():
+                so = oracle.step(p, opts, s)
+                if key == "o":
+                    iters_o.append(so.iterations)
+                    above_o += so.max_err / p.rest_density >= sc.threshold
+            if k % 10 == 9:
+                states = [(key, s["f_vel"], s["f_pos"]) for key, s in runs.items()]
+                states.append(("g", f.get_field("velocity"), f.get_field("position")))
+                for key, v, x in states:
+                    ke[key].append(kinetic_energy(p.particle_mass, v))
+                    com[key].append(np.asarray(x, np.float64).mean(0))
+        ke = {key: np.array(v) for key, v in ke.items()}
+        com = {key: np.array(v) for key, v in com.items()}
+        ke_max = max(ke_max, float(ke["o"].max()))
+        chaos_ke = max(np.abs(ke[f"b{r}"] - ke["o"]).max() for r in range(2))
+        chaos_com = max(np.abs(com[f"b{r}"] - com["o"]).max() for r in range(2))
+        gpu_ke, gpu_com = np.abs(ke["g"] - ke["o"]).max(), np.abs(com["g"] - com["o"]).max()
+        worst["ke"] = max(worst["ke"], gpu_ke / (3 * chaos_ke + 1e-3 * ke_max))
+        worst["com"] = max(worst["com"], gpu_com / (3 * chaos_com + 1e-5))
+        print(f"steps {seg * 100 + 1}-{seg * 100 + 100}: KE drift 1-ulp {chaos_ke / ke_max:.2e}, gpu "
+              f"{gpu_ke / ke_max:.2e}; COM drift 1-ulp {chaos_com:.2e} m, gpu {gpu_com:.2e} m")
+    f.close()
+    print(f"32K x 1000 steps: worst segment KE / bound {worst['ke']:.2f}, COM / bound {worst['com']:.2f}; mean "
+          f"iterations gpu {np.mean(iters_g):.3f} oracle {np.mean(iters_o):.3f}; steps above 1%: gpu {above_g}, "
+          f"oracle {above_o}")
+    assert worst["ke"] <= 1.0 and worst["com"] <= 1.0, worst
+    assert abs(np.mean(iters_g) - np.mean(iters_o)) < 0.5
+    assert above_g <= 5 and above_o <= 5

@@ -30,14 +30,19 @@ def _noalloc(keys, vals, n, max_bits):
 def test_noalloc_sort_matches_allocating_sort_twice():
     torch = pytest.importorskip("torch")
     rng = np.random.default_rng(2024)
-    ref_sorter = RadixSort(0)
-    # two calls in a row with different inputs: the second must not see anything left by the first
+    ref_sorter = None
+    # two calls in a row with different inputs: the second must not see anything left by the first. The
+    # first no-alloc call comes before the allocating sorter exists, so in a fresh process it is the call
+    # that finds the library's scratch with nothing else of the library set up on the device.
     for n, hi, bits in [(MAX, 1 << 19, 19), (300001, 1 << 32, 0)]:
         keys = rng.integers(0, hi, n, dtype=np.uint64).astype(np.uint32)
         vals = rng.integers(0, 1 << 32, n, dtype=np.uint64).astype(np.uint32)
         k1, v1 = _dev(keys.view(np.int32)), _dev(vals.view(np.int32))
         k2, v2 = k1.clone(), v1.clone()
         assert _noalloc(k1, v1, n, bits) == _lib.OK, _lib.load().pcisph_last_error()
+        torch.cuda.synchronize()
+        if ref_sorter is None:
+            ref_sorter = RadixSort(0)
         ref_sorter.enqueue(k2, v2, n, max_bits=bits)
         torch.cuda.synchronize()
         # integer results: exact agreement (tolerance zero)
@@ -53,3 +58,26 @@ def test_noalloc_sort_rejects_more_than_its_maximum():
     v = torch.zeros(MAX + 1, dtype=torch.int32, device="cuda")
     assert _noalloc(k, v, MAX + 1, 0) == _lib.ERR_INVALID_ARG
     assert b"exceed its fixed scratch" in _lib.load().pcisph_last_error()
+
+
+def test_noalloc_sort_argument_checks():
+    """Bad arguments come back as status codes before any work is queued; an empty sort is a no-op."""
+    torch = pytest.importorskip("torch")
+    L = _lib.load()
+    k = torch.arange(64, 0, -1, dtype=torch.int32, device="cuda")
+    v = torch.arange(64, dtype=torch.int32, device="cuda")
+    assert _noalloc(k, v, 64, 33) == _lib.ERR_INVALID_ARG
+    assert b"max_bits" in L.pcisph_last_error()
+    assert L.pcisph_radixsort_enqueue_noalloc(None, C.c_void_p(v.data_ptr()), 64, 0, None) == _lib.ERR_INVALID_ARG
+    assert L.pcisph_radixsort_enqueue_noalloc(C.c_void_p(k.data_ptr()), None, 64, 0, None) == _lib.ERR_INVALID_ARG
+    assert L.pcisph_radixsort_enqueue_noalloc(None, None, 0, 0, None) == _lib.OK
+    assert _noalloc(k, v, 0, 0) == _lib.OK
+    torch.cuda.synchronize()
+    # nothing was touched by the rejected or empty calls
+    np.testing.assert_array_equal(k.cpu().numpy(), np.arange(64, 0, -1))
+    np.testing.assert_array_equal(v.cpu().numpy(), np.arange(64))
+    # and the same array then sorts
+    assert _noalloc(k, v, 64, 7) == _lib.OK
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(k.cpu().numpy(), np.arange(1, 65))
+    np.testing.assert_array_equal(v.cpu().numpy(), np.arange(63, -1, -1))
