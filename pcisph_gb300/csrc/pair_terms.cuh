@@ -5,7 +5,8 @@
 //     sqrtf and division, and divisions by densities use __fdividef (<= 2 ulp). The reference itself uses
 //     fast_length, which OpenCL allows to be approximate. Errors stay near 1e-7 relative per term, far
 //     inside the 1e-5 parity bound; the cost per in-range pair drops from ~50 to ~10 instructions.
-//   - pairs with r^2 > h^2 are skipped: every reference kernel returns exactly 0 for them.
+//   - pairs with r^2 > h^2 are skipped: every reference kernel returns exactly 0 for them (the force term
+//     also looks at pairs within a few ulp beyond h, for its curvature cut-off: see force_term).
 #pragma once
 #include "common.cuh"
 
@@ -38,17 +39,24 @@ __device__ __forceinline__ void force_term(const float4& xi, const float3& vi, c
                                            ForceAccum& a) {
     const float dx = xi.x - o.x, dy = xi.y - o.y, dz = xi.z - o.z;
     const float r2 = dist2(dx, dy, dz);
-    if (r2 <= P.h2) {
+    // The curvature term does not vanish at r = h: it jumps to zero there. Within a few ulp of the cut-off the
+    // decision is taken on the length as the oracle forms it (dot product rounded term by term, correctly
+    // rounded sqrtf: its reading of the reference's fast_length), so that both land on the same side of h; a
+    // lattice at spacing h/2, like the reference's voxel scenes, has many pairs at r = h.
+    const bool at_cut = fabsf(r2 - P.h2) <= 1e-6f * P.h2;
+    if (r2 <= P.h2 || at_cut) {
         const float inv_r = r2 > 0.f ? rsqrtf(r2) : 0.f;
         const float dist = __fmul_rn(r2, inv_r);  // rounded once: it has several uses
         const float rj = o.w;
-        if (rj > 0.0001f) {
+        if (r2 <= P.h2 && rj > 0.0001f) {
             const float k = __fdividef(__fsub_rn(P.h, dist), rj);  // kernel_viscosity_d2 / rho_j
             a.visc.x += (vj.x - vi.x) * k;
             a.visc.y += (vj.y - vi.y) * k;
             a.visc.z += (vj.z - vi.z) * k;
         }
-        if (dist > 0.0001f && dist < P.h) {
+        const float d_cut =
+            at_cut ? __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz))) : dist;
+        if (dist > 0.0001f && d_cut < P.h) {
             const float corr = __fdividef(2.f * P.rest_density, xi.w + rj);
             const float c = corr * surface_tension_kernel(dist, P.h, P.st_term) * inv_r;  // * (x_i - x_j)/r
             a.coh.x += c * dx;

@@ -182,36 +182,65 @@ def test_two_blocks_8m_sort_and_sweeps(oracle):
     f.close()
 
 
-def test_boundary_1m_warmed_step(oracle):
-    """The 1M dam break against 284,192 boundary particles (the boundary workload: the reference's 3-7
-    iterations, per-particle skins on), one step from the state after three warm-up steps: fluid and boundary
-    keys, permutations and cell ranges bit-exact, equal iterations, every field within the bound above, the
-    boundary pressures too."""
-    sc = scenes.dam_break_1m_boundary()
+def _check_step_with_boundary(oracle, sc, f, label):
+    """One GPU step of context f (already holding sc's state) against the oracle's step from the same state:
+    fluid and boundary keys, permutations and cell ranges bit-exact, equal iterations, every field within the
+    bound above, the boundary pressures too."""
     B = sc.boundary_count
-    f = _fluid(sc)
-    f.step(3)
     pos, vel = f.get_field("position"), f.get_field("velocity")
     f.update()
     p = oracle.derive_params(sc.particle_radius, sc.rest_density, sc.fluid_count, B, sc.delta_t, sc.gravity,
                              sc.viscosity_constant(), sc.surface_tension)
     opts = make_options(threshold=sc.threshold, min_iters=sc.min_iters, max_iters=sc.max_iters, walls=sc.walls,
                         box_lo=sc.box_lo, box_hi=sc.box_hi, restitution=sc.restitution)
-    s32 = oracle.new_state(p, pos, vel, sc.boundary_pos)
-    st32 = oracle.step(p, opts, s32, boundary_sort=True)
-    s64 = oracle.new_state(p, pos, vel, sc.boundary_pos, dtype=np.float64)
-    st64 = oracle.step(p, opts, s64, boundary_sort=True)
+    bpos = sc.boundary_pos if B else None
+    s32 = oracle.new_state(p, pos, vel, bpos)
+    st32 = oracle.step(p, opts, s32, boundary_sort=bool(B))
+    s64 = oracle.new_state(p, pos, vel, bpos, dtype=np.float64)
+    st64 = oracle.step(p, opts, s64, boundary_sort=bool(B))
     eq = np.testing.assert_array_equal
-    eq(f.get_field("boundary_keys"), s32["b_keys"])
-    eq(f.get_field("boundary_src"), s32["b_src"])
-    eq(f.get_field("boundary_cell_offsets"), s32["b_off"])
-    _compare_step("1M + boundary step 4", _ctx_getter(f), f.stats(), p, s32, st32, s64, st64)
-    scale = p.density_variation_scaling_factor * p.rest_density * st32.iterations
-    e = rel_err(f.get_field("boundary_pressure"), s32["b_press"], scale)
-    print(f"boundary pressure: {e:.1e}")
-    if e > RTOL:  # as for the fluid fields: no farther from FP64 than 3x the FP32 oracle
-        e64 = rel_err(f.get_field("boundary_pressure"), s64["b_press"], scale)
-        assert st64.iterations == st32.iterations and e64 <= max(RTOL, 3 * rel_err(s32["b_press"], s64["b_press"], scale))
+    if B:
+        eq(f.get_field("boundary_keys"), s32["b_keys"])
+        eq(f.get_field("boundary_src"), s32["b_src"])
+        eq(f.get_field("boundary_cell_offsets"), s32["b_off"])
+    _compare_step(label, _ctx_getter(f), f.stats(), p, s32, st32, s64, st64)
+    if B:
+        scale = p.density_variation_scaling_factor * p.rest_density * st32.iterations
+        e = rel_err(f.get_field("boundary_pressure"), s32["b_press"], scale)
+        print(f"{label} boundary pressure: {e:.1e}")
+        if e > RTOL:  # as for the fluid fields: no farther from FP64 than 3x the FP32 oracle
+            e64 = rel_err(f.get_field("boundary_pressure"), s64["b_press"], scale)
+            own = rel_err(s32["b_press"], s64["b_press"], scale)
+            assert st64.iterations == st32.iterations and e64 <= max(RTOL, 3 * own)
+
+
+def test_boundary_1m_warmed_step(oracle):
+    """The 1M dam break against 284,192 boundary particles (the boundary workload: the reference's 3-7
+    iterations, per-particle skins on), one step from the state after three warm-up steps."""
+    sc = scenes.dam_break_1m_boundary()
+    f = _fluid(sc)
+    f.step(3)
+    _check_step_with_boundary(oracle, sc, f, "1M + boundary step 4")
+    f.close()
+
+
+@pytest.mark.parametrize("name,warm", [("dambreak", 0), ("dambreak", 2), ("cube_splash", 0), ("simple_drop", 0)])
+def test_reference_scenes_vs_oracle(oracle, name, warm):
+    """The reference's own voxel scenes at their own resolutions (decoded from the reference's .xraw files by
+    the loader that tests/test_xraw_cpu.py pins to the reference's: dambreak 279,936 fluid + 154,980 boundary
+    particles, cube_splash 438,976 + 322,272, simple_drop 27,000 without boundary) with the reference's
+    settings (scenes.cpp:217-245: dt 0.002 s, 3..7 iterations, no walls), stepped on the GPU with the
+    library's defaults and by the oracle from the same state: the scene's first step, and for dambreak also
+    its third."""
+    from pcisph_gb300 import xraw
+    import os
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "xraw_scenes.npz"))
+    grid = xraw.VoxelGrid(tuple(int(v) for v in g[f"{name}_size"]), g[f"{name}_voxels"])
+    sc = xraw.reference_scene(grid, name)
+    f = _fluid(sc)
+    if warm:
+        f.step(warm)
+    _check_step_with_boundary(oracle, sc, f, f"{name} step {warm + 1}")
     f.close()
 
 
@@ -257,10 +286,13 @@ def _ulp_nudged(pos, seed):
 def test_dam_break_32k_long_run_statistics(oracle):
     """The 32,768-particle dam break over its 1000 steps, GPU run against the oracle, in ten segments of 100
     steps. SPH trajectories are chaotic (two runs part at the level of single particles within ~100 steps), so
-    at the start of each segment the oracle takes the GPU run's state, and over the segment the GPU's kinetic
-    energy (every 10 steps) and centre of mass must stay within 3x the larger drift of two oracle runs from
-    that state with every coordinate moved by one ulp (seeded signs: the size of the rounding differences
-    between two FP32 implementations), plus floors of 1e-3 of the run's largest kinetic energy and 1e-5 m.
+    at the start of each segment the oracle takes the GPU run's state, and two more oracle runs take that state
+    with every coordinate moved by one ulp (seeded signs: the size of the rounding differences between two FP32
+    implementations). Over each segment the drift of a run from the oracle run is the largest difference in
+    kinetic energy (every 10 steps) and in centre of mass. Drifts are heavy-tailed (a segment with a splash
+    parts runs 10x further than a quiet one, and three runs from one state spread 4x), so the GPU's ten drifts
+    are compared with the twenty of the nudged runs as samples: median and maximum each within 3x, plus floors
+    of 1e-3 of the run's largest kinetic energy and 1e-5 m.
     Over the whole run: mean corrective iterations within 0.5, and the density-error gate: every step of the
     GPU run that ends above the 1% threshold ends there in the oracle too, stepped from the GPU's state before
     it (equal iterations, the same error within 1e-5 of rest density), and at most 0.5% of the steps of either
@@ -271,7 +303,7 @@ def test_dam_break_32k_long_run_statistics(oracle):
     f = _fluid(sc)
     iters_g, iters_o, above_g, above_o = [], [], 0, 0
     ke_max = 0.0
-    worst = {"ke": 0.0, "com": 0.0}
+    drift = {"g": {"ke": [], "com": []}, "b": {"ke": [], "com": []}}
     for seg in range(10):
         pos, vel = (sc.fluid_pos, np.zeros_like(sc.fluid_pos)) if seg == 0 else (f.get_field("position"),
                                                                                 f.get_field("velocity"))
@@ -305,17 +337,22 @@ def test_dam_break_32k_long_run_statistics(oracle):
         ke = {key: np.array(v) for key, v in ke.items()}
         com = {key: np.array(v) for key, v in com.items()}
         ke_max = max(ke_max, float(ke["o"].max()))
-        chaos_ke = max(np.abs(ke[f"b{r}"] - ke["o"]).max() for r in range(2))
-        chaos_com = max(np.abs(com[f"b{r}"] - com["o"]).max() for r in range(2))
-        gpu_ke, gpu_com = np.abs(ke["g"] - ke["o"]).max(), np.abs(com["g"] - com["o"]).max()
-        worst["ke"] = max(worst["ke"], gpu_ke / (3 * chaos_ke + 1e-3 * ke_max))
-        worst["com"] = max(worst["com"], gpu_com / (3 * chaos_com + 1e-5))
-        print(f"steps {seg * 100 + 1}-{seg * 100 + 100}: KE drift 1-ulp {chaos_ke / ke_max:.2e}, gpu "
-              f"{gpu_ke / ke_max:.2e}; COM drift 1-ulp {chaos_com:.2e} m, gpu {gpu_com:.2e} m")
+        for key in ("g", "b0", "b1"):
+            d = drift[key[0]]
+            d["ke"].append(np.abs(ke[key] - ke["o"]).max())
+            d["com"].append(np.abs(com[key] - com["o"]).max())
+        print(f"steps {seg * 100 + 1}-{seg * 100 + 100}: KE drift 1-ulp {drift['b']['ke'][-2] / ke_max:.2e} "
+              f"{drift['b']['ke'][-1] / ke_max:.2e}, gpu {drift['g']['ke'][-1] / ke_max:.2e}; COM drift 1-ulp "
+              f"{drift['b']['com'][-2]:.2e} {drift['b']['com'][-1]:.2e} m, gpu {drift['g']['com'][-1]:.2e} m")
     f.close()
-    print(f"32K x 1000 steps: worst segment KE / bound {worst['ke']:.2f}, COM / bound {worst['com']:.2f}; mean "
-          f"iterations gpu {np.mean(iters_g):.3f} oracle {np.mean(iters_o):.3f}; steps above 1%: gpu {above_g}, "
-          f"oracle {above_o}")
-    assert worst["ke"] <= 1.0 and worst["com"] <= 1.0, worst
+    ratios = {}
+    for q, floor in (("ke", 1e-3 * ke_max), ("com", 1e-5)):
+        g, b = np.array(drift["g"][q]), np.array(drift["b"][q])
+        ratios[q + " median"] = np.median(g) / (3 * np.median(b) + floor)
+        ratios[q + " max"] = g.max() / (3 * b.max() + floor)
+    print("32K x 1000 steps, GPU drift / bound: " + ", ".join(f"{k} {v:.2f}" for k, v in ratios.items()) +
+          f"; mean iterations gpu {np.mean(iters_g):.3f} oracle {np.mean(iters_o):.3f}; steps above 1%: gpu "
+          f"{above_g}, oracle {above_o}")
+    assert all(v <= 1.0 for v in ratios.values()), ratios
     assert abs(np.mean(iters_g) - np.mean(iters_o)) < 0.5
     assert above_g <= 5 and above_o <= 5
