@@ -166,6 +166,62 @@ def test_kernel_chain_vs_reference(golden, case, variant):
     print(case, variant, {k: f"{v:.1e}" for k, v in errs.items()})
 
 
+@pytest.mark.parametrize("variant", [0, 1, 2])
+def test_force_curvature_cut_off_vs_oracle(oracle, variant):
+    """pcisph.cl:152-158: the cohesion and curvature terms switch on for r < h, and the curvature term does
+    not vanish there, so a pair at r = h adds a finite term on one side of the cut-off and nothing on the
+    other. An unjittered lattice at spacing h/2 holds thousands of pairs at r = h; every coordinate moved by
+    one ulp (seeded signs) puts them on both sides by a few ulp, and random normals make the curvature term of
+    every pair non-zero. The force stage on these inputs must side with the FP32 oracle on every pair: other
+    force within 2e-6 normwise (the gravity-free part's scale), where one pair decided the other way moves a
+    particle's force by a whole curvature term."""
+    sc = scenes.small_dam(12)
+    d = 0.02
+    pos = scenes.lattice_block(12, 12, 12, d, (0.0, 0.0, 0.0), seed=0, jitter=0)
+    rng = np.random.default_rng(11)
+    up = rng.integers(0, 2, pos.shape).astype(bool)
+    pos = np.where(up, np.nextafter(pos, np.float32(np.inf)), np.nextafter(pos, np.float32(-np.inf)))
+    N = pos.shape[0]
+    p0 = oracle.derive_params(sc.particle_radius, sc.rest_density, N, 0, sc.delta_t, sc.gravity,
+                              sc.viscosity_constant(), sc.surface_tension)
+    f = fluid_like(p0, kernel_variant=variant)
+    got = np.frombuffer(bytes(f.get_params()), np.int32).astype(np.int64)
+    assert np.all(np.abs(got - np.frombuffer(bytes(p0), np.int32)) <= 1)  # the library derives the same
+    p = p0
+    f.set_fluid_state(pos, rng.uniform(-0.1, 0.1, (N, 3)).astype(np.float32))
+    f.run_stage("sort")
+    f.run_stage("density")
+    sp, sv = f.get_field("sorted_position"), f.get_field("sorted_velocity")
+    off = f.get_field("cell_offsets")
+    rho = (p.rest_density * (1.0 + rng.uniform(-0.01, 0.01, N))).astype(np.float32)
+    f.set_field("density", rho)
+    f.run_stage("pack")
+    f.run_stage("normal")
+    nrm = (rng.uniform(-1.0, 1.0, (N, 3)) * np.abs(f.get_field("normal")).max()).astype(np.float32)
+    f.set_field("normal", nrm)
+    f.run_stage("force")
+    got = f.get_field("other_force")
+    f.close()
+    want, _, _ = oracle.force_init(p, off, sp, nrm, rho, sv)
+
+    # the pairs near the cut-off, with their length formed as the oracle forms it
+    h = np.float32(p.kernel_radius)
+    i, j = np.triu_indices(N, 1)
+    dx = sp[i] - sp[j]
+    r2 = (dx[:, 0] * dx[:, 0] + dx[:, 1] * dx[:, 1]) + dx[:, 2] * dx[:, 2]
+    near = np.abs(r2 - h * h) <= np.float32(1e-6) * h * h
+    r = np.sqrt(r2[near])
+    assert near.sum() >= 2500 and (r < h).sum() >= 300 and (r >= h).sum() >= 300, (near.sum(), (r < h).sum())
+    fragile = np.abs(r - h) <= 2 * np.spacing(h)  # where a length off by 2 ulp flips the decision
+    assert fragile.sum() >= 300, fragile.sum()
+
+    g = np.array([0.0, p.particle_mass * p.gravity, 0.0], np.float32)
+    e = rel_err(got, want, scale=np.abs(want - g).max())
+    print(f"variant {variant}: {near.sum()} pairs within 1e-6 of h^2 ({fragile.sum()} within 2 ulp of h), "
+          f"other force {e:.1e}")
+    assert e <= 2e-6
+
+
 @pytest.mark.parametrize("variant", [1, 2])
 @pytest.mark.parametrize("case", ["step_boundary", "step_dambreak"])
 def test_boundary_self_density_computed(golden, case, variant):
