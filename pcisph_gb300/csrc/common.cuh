@@ -38,6 +38,10 @@ struct DevParams {
     // its neighbourhood walk (as with one skin). 0: every particle has skin_max_half (half the list skin).
     int particle_skin;
     float skin_min_half, skin_max_half, skin_factor;
+    // partner marks (one scene, list sweeps): a prediction round with at most mark_cap fast predictions lists
+    // them, and a kernel stamps the particles whose pressure sweep must walk because of them; 0: off (every
+    // particle near a flagged bucket walks)
+    uint32_t mark_cap;
     // batched scenes with an adaptive skin: each step picks one of kSkinLevels skins from the previous
     // step's count of predictions past each level's half skin (skin_half[k])
     int adaptive_skin;
@@ -71,6 +75,11 @@ struct Control {
     unsigned long long over_level[3];  // adaptive skin: this step's predictions past each level's half skin
     unsigned long long unconverged_steps;  // steps that ended at max_iters with the variation above threshold
     unsigned int max_err_max_bits;         // float bits of the largest end-of-step max variation / rest density
+    // partner marks (DevParams::mark_cap): fast predictions of the current round (those below mark_cap are in
+    // the fast list), and the number of prediction rounds closed (round + 1 stamps the particles that walk in
+    // the current round's pressure sweep, whose last block closes the round)
+    unsigned long long fast_n;
+    unsigned int round;
 };
 
 // Close a step after its last corrective iteration `it` (Fluid.cpp:301-306 decides the same way): status

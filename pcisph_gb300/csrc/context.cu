@@ -115,16 +115,22 @@ struct pcisph_ctx {
     bool working_order() const {
         return list_sweeps() && (opts.spatial_order == 1 || (opts.spatial_order == 2 && params.fluid_count >= (1u << 17)));
     }
-    ListBuffers list_buffers() const {
+    // marks: the launch follows the partner-marking kernel of its round (the graph's and the host-driven
+    // loop's pressure sweeps, and that kernel itself): the pressure sweep may read the stamps
+    ListBuffers list_buffers(bool marks = false) const {
         const bool w = working_order();
+        const bool m = P.mark_cap != 0;
         return ListBuffers{b.pos, b.vel, b.pr4, b.normal, b.f_other, b.f_press, b.pred, b.pf4, b.state_pos,
                            b.state_vel, b.rho, b.press, b.err, w ? cells_w : b.cells, b.b_cells, b.b_pos, b.bpf,
                            b.nbr, b.nbr_count, b.near, b.near_count, b.bucket_fast, P.fluid_count,
                            w ? d_of_w : nullptr, b.disp_max, b.state_skin, b.b_init, b.b_press, b.b_near, b.bnbr,
                            b.bnbr_count, b.bfl,
                            b.bfl_count, zone_map, {zone_org[0], zone_org[1], zone_org[2]},
-                           {zone_dim[0], zone_dim[1], zone_dim[2]}};
+                           {zone_dim[0], zone_dim[1], zone_dim[2]}, m ? b.fast_list : nullptr,
+                           m && marks ? b.walk_stamp : nullptr};
     }
+    // the partner-marking kernel runs after each prediction round of the graph and the host-driven loop
+    bool partner_marks() const { return list_sweeps() && P.mark_cap != 0 && opts.loop_mode != 2; }
 
     // Working-order buffers for n particles and bk buckets; the index maps start as the identity.
     int ensure_order() {
@@ -211,6 +217,7 @@ struct pcisph_ctx {
         const bool bnd = nb > 0;
         const size_t bytes = align256(n * P.list_cap * 4) + align256(n * 4) + align256(n * P.near_cap * 4) +
                              align256(n * 4) + align256(params.bucket_count) + align256(n) +
+                             align256((size_t)kMarkCap * 4) + align256(n * 4) +
                              (bnd ? align256(n * P.bnd_cap * 4) + align256(n * 4) + align256(nb * P.bfl_cap * 4) +
                                         align256(nb * 4)
                                   : 0);
@@ -225,6 +232,9 @@ struct pcisph_ctx {
         b.near_count = c.take<uint32_t>(n);
         b.bucket_fast = c.take<unsigned char>(params.bucket_count);
         b.b_near = c.take<unsigned char>(n);
+        b.fast_list = c.take<uint32_t>(kMarkCap);
+        b.walk_stamp = c.take<uint32_t>(n);
+        CUDA_TRY(cudaMemsetAsync(b.walk_stamp, 0, n * 4, stream()));  // round numbers start at 1
         b.bnbr = bnd ? c.take<uint32_t>(n * P.bnd_cap) : nullptr;
         b.bnbr_count = bnd ? c.take<uint32_t>(n) : nullptr;
         b.bfl = bnd ? c.take<uint32_t>(nb * P.bfl_cap) : nullptr;
@@ -345,6 +355,10 @@ struct pcisph_ctx {
         P.particle_skin = skins && list_sweeps() ? 1 : 0;
         P.skin_min_half = std::min(kSkinMinHalf * P.h, P.skin_max_half);
         P.skin_factor = kSkinFactor;
+        // partner marks scan the 5 x 5 x 5 cells around a fast prediction: a particle that did not outrun its
+        // skin lies within h + skin_max_half of a prediction within h of its own, which must stay below two
+        // cells (with a margin for the divisions of cell_of)
+        P.mark_cap = list_sweeps() && P.h + P.skin_max_half <= 1.9f * P.cell_size ? kMarkCap : 0u;
         graph_valid = false;
         order_age = kNoOrder;
     }
@@ -499,6 +513,10 @@ struct pcisph_ctx {
         else if (warp_sweeps()) timed("force", s, [&] { launch_force_sweep(P, b, A, sweep_grid, s); });
         else timed("force", s, [&] { launch_force(P, b, s); });
         nl += 4;
+        if (partner_marks()) {
+            timed("mark", s, [&] { launch_mark_partners(P, b.ctl, list_buffers(true), s); });
+            ++nl;
+        }
         if (cudaGetLastError() != cudaSuccess) return -1;
         return nl;
     }
@@ -513,10 +531,15 @@ struct pcisph_ctx {
             ++nl;
         }
         if (list_sweeps()) {
-            timed("pressure", s, [&] { launch_pressure_list(P, b.ctl, list_buffers(), opts.sweep_block, s); });
+            const bool marks = partner_marks();
+            timed("pressure", s, [&] { launch_pressure_list(P, b.ctl, list_buffers(marks), opts.sweep_block, s); });
             timed("pressure_force", s, [&] {
                 launch_pressure_force_list(P, b.ctl, list_buffers(), 0, cond, use_cond, opts.sweep_block, s);
             });
+            if (marks) {
+                timed("mark", s, [&] { launch_mark_partners(P, b.ctl, list_buffers(true), s); });
+                ++nl;
+            }
         } else if (warp_sweeps()) {
             const SweepArgs A = sweep_args();
             timed("pressure", s, [&] { launch_pressure_sweep(P, b, A, sweep_grid, s); });

@@ -35,6 +35,8 @@ inline constexpr uint32_t kListCap = 96;           // neighbour-list entries per
 inline constexpr uint32_t kNearCap = 64;           // within-h list entries per particle
 inline constexpr uint32_t kBoundaryListCap = 48;   // boundary particles within r_list per fluid particle
 inline constexpr uint32_t kBoundaryFluidCap = 64;  // fluid particles within r_list per boundary particle
+// partner marks: fast predictions a round may list (more: the round walks by bucket flags)
+inline constexpr uint32_t kMarkCap = 65536;
 // skin-list entries per particle of a batch (skins up to 0.5 h: ~48 (1 + skin)^3 entries at rest density)
 inline constexpr uint32_t kListCapWide = 168;
 // adaptive skin: a level qualifies if at most 1 in this many of the last step's predictions outran it

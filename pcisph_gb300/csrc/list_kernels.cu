@@ -45,6 +45,7 @@ namespace {
 
 constexpr int kBlock = 256;
 inline unsigned grid_for(uint32_t n) { return (n + kBlock - 1) / kBlock; }
+constexpr unsigned kMarkBlocks = 152;  // the marking kernel's grid (grid-stride over its items)
 
 // List layout: entries k = 8c .. 8c+7 of particle i (chunk c) are 32 contiguous bytes at uint4 offset
 // 2 (c * stride + i); chunks are column-major over particles. A warp's 32 consecutive particles read
@@ -329,8 +330,72 @@ __global__ void __launch_bounds__(kBlock) k_force_list(PS ps, ListBuffers b) {
     const float3 dx = v * P.dt;
     const float4 xs = make_float4(xi.x + dx.x, xi.y + dx.y, xi.z + dx.z, 0.f);
     b.pred[i] = xs;
-    const float disp = note_displacement(P, ps.control(i), b.bucket_fast, xi, xs, P.list_half_skin);
+    const float disp = note_displacement(P, ps.control(i), b.bucket_fast, xi, xs, P.list_half_skin,
+                                         PS::kBatched ? nullptr : b.fast_list, i);
     if (P.particle_skin) b.disp_max[i] = disp;
+}
+
+// Partner marks after a prediction round (one scene). A pair of the reference's walk whose predictions are
+// within h is in the skin list unless one of the two predictions is fast (moved more than half the skin), so
+// the pressure sweep of particle i can use its list unless i is fast or some fast j has x*_j within h of
+// x*_i while j is not in i's list. For every fast j of the round (the fast list), thread (j, o) takes cell o
+// of the 5 x 5 x 5 cells around x*_j's cell: a particle i that is not fast lies within
+// D = h + skin_max_half (< 2 cells, checked on the host) of x*_j, so its cell is among them, and only the
+// cells whose box comes within D of x*_j (with a margin for the divisions of cell_of) are scanned. It stamps i
+// with the round's number when |x*_i - x*_j| <= h (the pressure sweep's |d|^2, with d negated: the same bits)
+// and |x_i - x_j| is beyond i's list radius (the builder's test, the same bits), and stamps j itself.
+// Stamping more than needed only makes a particle walk, which gives the walk's sum. The round is the one the
+// next pressure sweep reads (Control::round + 1); that sweep's last block closes it. A round with more than
+// mark_cap fast predictions stamps nothing (the sweep then uses the bucket flags).
+__global__ void __launch_bounds__(kBlock) k_mark_partners(DevParams P, const Control* ctl, ListBuffers b) {
+    const unsigned long long n = ctl->fast_n;
+    if (n == 0 || n > P.mark_cap) return;
+    const unsigned round = ctl->round + 1u;
+    const float reach = P.h + P.skin_max_half + 0.01f * P.cell_size;
+    const unsigned long long items = n * 125ull;
+    for (unsigned long long t = (unsigned long long)blockIdx.x * kBlock + threadIdx.x; t < items;
+         t += (unsigned long long)gridDim.x * kBlock) {
+        const uint32_t j = b.fast_list[t / 125ull];
+        const uint32_t o = (uint32_t)(t % 125ull);
+        if (o == 62u) b.walk_stamp[j] = round;  // the centre cell's thread: j itself walks
+        const float4 pj = b.pred[j];
+        const float4 xj = b.pos[j];
+        const Cell c0 = cell_of(pj.x, pj.y, pj.z, P);
+        const int off[3] = {(int)(o % 5u) - 2, (int)(o / 5u % 5u) - 2, (int)(o / 25u) - 2};
+        const uint32_t cc[3] = {c0.x + (uint32_t)off[0], c0.y + (uint32_t)off[1], c0.z + (uint32_t)off[2]};
+        // Skip a cell whose box is farther than the reach from x*_j. Within 2^14 cells of the origin the
+        // rounding of the box bounds and of cell_of's division is far below the margin in the reach; farther
+        // out (or saturated, or NaN) every cell is scanned.
+        auto inner = [](uint32_t c) { return c + 16384u < 32768u; };  // -2^14 < (int)c < 2^14, wrapping
+        if (inner(c0.x) && inner(c0.y) && inner(c0.z)) {
+            const float pc[3] = {pj.x, pj.y, pj.z};
+            float gap2 = 0.f;  // squared distance from x*_j to the cell's box
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                const float lo = (float)(int)cc[a] * P.cell_size, hi = lo + P.cell_size;
+                const float g = fmaxf(fmaxf(lo - pc[a], pc[a] - hi), 0.f);
+                gap2 += g * g;
+            }
+            if (gap2 > reach * reach) continue;
+        }
+        const uint2 r = b.cells[P.bucket_base + hash_key(cc[0], cc[1], cc[2], P)];
+#pragma unroll 1
+        for (uint32_t i0 = r.x; i0 < r.y; i0 += 4) {
+            float4 pi[4], xi[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                if (i0 + u < r.y) {
+                    pi[u] = b.pred[i0 + u];
+                    xi[u] = b.pos[i0 + u];
+                }
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                if (i0 + u < r.y && dist2(pj.x - pi[u].x, pj.y - pi[u].y, pj.z - pi[u].z) <= P.h2 &&
+                    !(dist2(xi[u].x - xj.x, xi[u].y - xj.y, xi[u].z - xj.z) <=
+                      particle_list_r2(P, half_skin_of(P, xi[u].w))))
+                    b.walk_stamp[i0 + u] = round;
+        }
+    }
 }
 
 // pcisph.cl:212-263 (boundary_update = 0); one scene: also the stop decision in the last block
@@ -371,8 +436,19 @@ __device__ __forceinline__ float pressure_body(const PS& ps, const ListBuffers& 
         }
         Cell c{0u, 0u, 0u};  // the cell (three IEEE divisions) only where a walk may need it
         const bool own_walk = overflow || (P.particle_skin && self_fast);
-        if (own_walk || !all_lists_ok || walk_boundary) c = cell_of(xi.x, xi.y, xi.z, P);
-        const bool walk = own_walk || (!all_lists_ok && near_fast(P, b.bucket_fast, c));
+        // partner marks of this round (one scene, after the marking kernel): the particles that may miss a
+        // pair of their walk are stamped with the round's number; a round past the cap (or no marks) takes
+        // the bucket flags: every particle near a fast one walks
+        const unsigned long long fast_round = !PS::kBatched && b.walk_stamp ? ctl->fast_n : ~0ull;
+        const bool marks = fast_round <= P.mark_cap;
+        bool walk;
+        if (marks) {
+            walk = own_walk || (fast_round != 0 && b.walk_stamp[i] == ctl->round + 1u);
+            if (walk || walk_boundary) c = cell_of(xi.x, xi.y, xi.z, P);
+        } else {
+            if (own_walk || !all_lists_ok || walk_boundary) c = cell_of(xi.x, xi.y, xi.z, P);
+            walk = own_walk || (!all_lists_ok && near_fast(P, b.bucket_fast, c));
+        }
         auto fb = [&](uint32_t j) { acc += density_term(xp.x, xp.y, xp.z, __ldg(&b.b_pos[j]), P.h2); };
         if (walk_boundary) for_each_neighbour(b.b_cells, c, P, fb);
         else if (list_boundary) for_each_listed(b.bnbr, i, bcnt, b.nbr_stride, fb);
@@ -431,6 +507,10 @@ __global__ void __launch_bounds__(BS) k_pressure_list(PS ps, ListBuffers b) {
     if (is_last && threadIdx.x == 0) {
         __threadfence();
         ctl->max_err_bits = atomicAdd(&ctl->max_err_bits, 0u);  // see every block's contribution
+        if (b.walk_stamp) {  // close the prediction round of the partner marks: the next one starts empty
+            ctl->round += 1u;
+            ctl->fast_n = 0;
+        }
         decide(ps.params(0), ctl);
     }
 }
@@ -472,7 +552,8 @@ __device__ __forceinline__ void pressure_force_body(const PS& ps, const ListBuff
     if (!integrate) {
         const float4 xs = f4(x, 0.f);
         b.pred[i] = xs;
-        const float disp = note_displacement(P, ctl, b.bucket_fast, xi, xs, P.list_half_skin);
+        const float disp = note_displacement(P, ctl, b.bucket_fast, xi, xs, P.list_half_skin,
+                                             PS::kBatched ? nullptr : b.fast_list, i);
         if (P.particle_skin) b.disp_max[i] = fmaxf(b.disp_max[i], disp);
         return;
     }
@@ -680,6 +761,9 @@ void launch_pressure_list(const DevParams& P, Control* ctl, const ListBuffers& b
     if (block == 128) k_pressure_list<OneScene, 128><<<(n + 127) / 128, 128, 0, s>>>(ps, b);
     else if (block == 512) k_pressure_list<OneScene, 512><<<(n + 511) / 512, 512, 0, s>>>(ps, b);
     else k_pressure_list<OneScene, kBlock><<<grid_for(n), kBlock, 0, s>>>(ps, b);
+}
+void launch_mark_partners(const DevParams& P, Control* ctl, const ListBuffers& b, cudaStream_t s) {
+    k_mark_partners<<<kMarkBlocks, kBlock, 0, s>>>(P, ctl, b);
 }
 void launch_pressure_force_list(const DevParams& P, Control* ctl, const ListBuffers& b, int mode,
                                 cudaGraphConditionalHandle cond, bool use_cond, int block, cudaStream_t s) {

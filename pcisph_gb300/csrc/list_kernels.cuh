@@ -42,6 +42,11 @@ struct ListBuffers {
     const unsigned char* b_zone;
     int zone_org[3];
     uint32_t zone_dim[3];
+    // partner marks (one scene, or null): the fast predictions of the round (DevParams::mark_cap entries), and
+    // per particle the last round in which the marking kernel stamped it to walk. walk_stamp is null in the
+    // launches that do not follow a marking kernel (the stage runner, the persistent loop).
+    uint32_t* fast_list;
+    uint32_t* walk_stamp;
 };
 
 // Is the cell in the boundary zone (ListBuffers::b_zone)? Cells are the signed integers the reference's
@@ -96,6 +101,10 @@ void launch_boundary_zone(const DevParams& P, const float4* b_pos, const int* or
 void launch_boundary_pressure_list(const DevParams& P, Control* ctl, const ListBuffers& b, cudaStream_t s);
 void launch_normal_list(const DevParams& P, Control* ctl, const ListBuffers& b, cudaStream_t s);
 void launch_force_list(const DevParams& P, Control* ctl, const ListBuffers& b, cudaStream_t s);
+// Partner marks of the prediction round just completed (DevParams::mark_cap; b.fast_list and b.walk_stamp
+// set): the particles whose next pressure sweep must walk. That sweep (launched with b.walk_stamp) closes
+// the round.
+void launch_mark_partners(const DevParams& P, Control* ctl, const ListBuffers& b, cudaStream_t s);
 // block: threads per block of the two corrective-loop sweeps (128, 256 or 512)
 void launch_pressure_list(const DevParams& P, Control* ctl, const ListBuffers& b, int block, cudaStream_t s);
 // mode 0: the loop decision picks predict or integrate; 1: predict; 2: integrate

@@ -96,6 +96,7 @@ __global__ void k_begin(Control* ctl) {
     ctl->guard_iters = 0;
     ctl->n_groups = 0;
     ctl->fast_at_begin = ctl->fast_particles;
+    ctl->fast_n = 0;
 }
 
 // pcisph.cl:65-92

@@ -36,6 +36,8 @@ struct StepBuffers {
     uint32_t* bnbr_count;            // entries per particle; > bnd_cap means "walk the boundary buckets"
     uint32_t* bfl;                   // per boundary particle: fluid particles within the list radius
     uint32_t* bfl_count;             // entries per boundary particle; > bfl_cap means "walk"
+    uint32_t* fast_list;             // partner marks: the round's fast predictions (mark_cap entries)
+    uint32_t* walk_stamp;            // partner marks: per particle, the last round that stamped it to walk
     // boundary
     float4 *b_pos, *bpf;
     float *b_press, *b_init;

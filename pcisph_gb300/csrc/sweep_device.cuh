@@ -1,6 +1,5 @@
-// sweep_device.cuh -- device helpers shared by the neighbour-list sweeps (list_kernels.cu) and the
-// cell-group sweeps (group_kernels.cu): warp-aggregated counters, the fast-prediction bookkeeping and the
-// corrective loop's decision.
+// sweep_device.cuh -- device helpers of the neighbour-list sweeps (list_kernels.cu): warp-aggregated
+// counters, the fast-prediction bookkeeping and the corrective loop's decision.
 #pragma once
 #include "common.cuh"
 
@@ -28,15 +27,33 @@ __device__ __forceinline__ void warp_count(unsigned long long* addr, bool pred) 
 // After predicting x*_i (stored as xs): a fast particle (moved more than half the skin) flags its bucket
 // and is counted (one atomic per warp that has one; no store otherwise: in a splash most predictions are
 // fast, and a flag stored by each of their warps measured slower than the counts alone); the predictions
-// past each adaptive skin level are counted.
+// past each adaptive skin level are counted. With a fast list (partner marks, one scene), a fast particle
+// also takes a slot of the round's list while the round holds at most P.mark_cap of them (one atomic per
+// warp that has one; none once the round is past the cap, which then falls back to the bucket flags).
 // Returns the displacement |x* - x|; threshold: the particle's fast_threshold.
 __device__ __forceinline__ float note_displacement(const DevParams& P, Control* ctl,
                                                    unsigned char* __restrict__ bucket_fast, const float4& xi,
-                                                   const float4& xs, float threshold) {
+                                                   const float4& xs, float threshold,
+                                                   uint32_t* __restrict__ fast_list = nullptr, uint32_t i = 0) {
     const float dx = xs.x - xi.x, dy = xs.y - xi.y, dz = xs.z - xi.z;  // exact: xs and xi are close
     const float disp = sqrtf(dist2(dx, dy, dz));
     const bool fast = disp > threshold;
     warp_count(&ctl->fast_particles, fast);
+    if (fast_list) {
+        const unsigned act = __activemask();
+        const unsigned set = __ballot_sync(act, fast);
+        if (set) {
+            const int lane = (int)(threadIdx.x & 31), leader = __ffs(set) - 1;
+            unsigned long long base = ~0ull;
+            if (lane == leader && *(volatile unsigned long long*)&ctl->fast_n <= P.mark_cap)
+                base = atomicAdd(&ctl->fast_n, (unsigned long long)__popc(set));
+            base = __shfl_sync(act, base, leader);
+            if (fast && base != ~0ull) {
+                const unsigned long long slot = base + __popc(set & ((1u << lane) - 1u));
+                if (slot < P.mark_cap) fast_list[slot] = i;
+            }
+        }
+    }
     if (P.adaptive_skin) {
 #pragma unroll
         for (int k = 0; k < kSkinLevels; ++k) warp_count(&ctl->over_level[k], disp > P.skin_half[k]);

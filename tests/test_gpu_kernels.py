@@ -424,27 +424,37 @@ def test_setters_zero_velocities_like_the_reference():
     np.testing.assert_array_equal(out[0], out[1])
 
 
-def test_list_sweeps_exact_with_fast_particles(oracle):
+@pytest.mark.parametrize("speed", [8.0, 40.0])
+def test_list_sweeps_exact_with_fast_particles(oracle, speed):
     """Neighbour lists (variant 2) drop only pairs that contribute zero, also when some particles move more
-    than half the list skin in one step (those flag their bucket, and particles near a flagged bucket walk
-    the 27 buckets). Against the walking variant (1) and the oracle, from identical state, fixed iterations."""
+    than half the list skin in one prediction. In the graph's and the host-driven loop (modes 0, 1) the
+    partner marks make a fast particle walk, and every particle its prediction reaches within h without
+    listing it; the persistent loop (mode 2) walks every particle near a fast particle's bucket. At ~8 m/s a
+    fast prediction moves ~0.2 h (past half the skin, not into an unlisted pair); at ~40 m/s ~h, into pairs
+    the lists do not hold. The three loops must agree bit for bit, and with the walking variant (1) and the
+    oracle, from identical state, fixed iterations."""
     sc = scenes.small_dam(14, seed=9)
     rng = np.random.default_rng(9)
     vel = (rng.standard_normal((sc.fluid_count, 3)) * 0.05).astype(np.float32)
     fast = rng.choice(sc.fluid_count, 25, replace=False)
-    vel[fast] = rng.standard_normal((25, 3)).astype(np.float32) * 8.0  # ~8 m/s: dt |v| >> skin h / 2
+    vel[fast] = rng.standard_normal((25, 3)).astype(np.float32) * speed  # dt |v| >> skin h / 2
     p = oracle.derive_params(sc.particle_radius, sc.rest_density, sc.fluid_count, 0, sc.delta_t, sc.gravity,
                              sc.viscosity_constant(), sc.surface_tension)
+    names = ("density", "pressure", "pressure_force", "position", "velocity", "density_variation")
     out = {}
-    for variant in (1, 2):
-        f = fluid_like(p, min_iters=5, max_iters=5, walls=True, box_hi=sc.box_hi, kernel_variant=variant)
+    for variant, loop_mode in ((1, 0), (2, 0), (2, 1), (2, 2)):
+        f = fluid_like(p, min_iters=5, max_iters=5, walls=True, box_hi=sc.box_hi, kernel_variant=variant,
+                       loop_mode=loop_mode)
         f.set_fluid_state(sc.fluid_pos, vel)
         f.update()
         st = f.stats()
         if variant == 2:
             assert st.fast_particles > 0 and st.list_fallbacks > 0, (st.fast_particles, st.list_fallbacks)
-        out[variant] = {n: f.get_field(n) for n in ("density", "pressure", "pressure_force", "position",
-                                                    "velocity", "density_variation")}
+        out[variant if loop_mode == 0 else (variant, loop_mode)] = {n: f.get_field(n) for n in names}
+        f.close()
+    for mode in (1, 2):
+        for n in names:
+            np.testing.assert_array_equal(out[(2, mode)][n], out[2][n], err_msg=f"loop mode {mode}: {n}")
     opts = make_options(threshold=0.01, min_iters=5, max_iters=5, walls=True, box_hi=sc.box_hi)
     s = oracle.new_state(p, sc.fluid_pos, vel)
     oracle.step(p, opts, s)
