@@ -424,6 +424,37 @@ def test_setters_zero_velocities_like_the_reference():
     np.testing.assert_array_equal(out[0], out[1])
 
 
+def test_partner_marks_past_their_cap_fall_back_to_bucket_flags(oracle):
+    """A round with more fast predictions than the fast list holds (64K) stamps nothing, and its pressure
+    sweep walks every particle near a flagged bucket, as the persistent loop always does. A 74,088-particle
+    block moving at ~20 m/s (~h/2 per prediction) makes every prediction fast: the three loops agree bit for
+    bit, and with the walking variant within 1e-5."""
+    sc = scenes.dam_break(42, extent=0.7)
+    rng = np.random.default_rng(4)
+    vel = (rng.standard_normal((sc.fluid_count, 3)) * 2.0 + np.array([20.0, 0.0, 0.0])).astype(np.float32)
+    p = oracle.derive_params(sc.particle_radius, sc.rest_density, sc.fluid_count, 0, sc.delta_t, sc.gravity,
+                             sc.viscosity_constant(), sc.surface_tension)
+    names = ("density", "pressure", "pressure_force", "position", "velocity", "density_variation")
+    out = {}
+    for variant, loop_mode in ((1, 0), (2, 0), (2, 1), (2, 2)):
+        f = fluid_like(p, min_iters=5, max_iters=5, walls=True, box_hi=sc.box_hi, kernel_variant=variant,
+                       loop_mode=loop_mode)
+        f.set_fluid_state(sc.fluid_pos, vel)
+        f.update()
+        if variant == 2:
+            st = f.stats()
+            assert st.fast_particles > 5 * 65536 and st.list_fallbacks == 5, (st.fast_particles, st.list_fallbacks)
+        out[(variant, loop_mode)] = {n: f.get_field(n) for n in names}
+        f.close()
+    for mode in (1, 2):
+        for n in names:
+            np.testing.assert_array_equal(out[(2, mode)][n], out[(2, 0)][n], err_msg=f"loop mode {mode}: {n}")
+    for n in names:
+        scale = p.density_variation_scaling_factor * p.rest_density * 5 if n == "pressure" else (
+            p.rest_density if n == "density_variation" else None)
+        assert rel_err(out[(2, 0)][n], out[(1, 0)][n], scale) <= 1e-5, n
+
+
 @pytest.mark.parametrize("speed", [8.0, 40.0])
 def test_list_sweeps_exact_with_fast_particles(oracle, speed):
     """Neighbour lists (variant 2) drop only pairs that contribute zero, also when some particles move more
