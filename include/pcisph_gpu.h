@@ -118,7 +118,8 @@ typedef struct pcisph_step_stats {
     uint64_t steps;              /* steps done by this context */
     uint64_t total_iterations;   /* corrective iterations summed over those steps */
     uint64_t list_fallbacks;     /* variant 2: pressure sweeps in which some predicted displacement exceeded
-                                    half the list skin (the particles near it walked the buckets) */
+                                    half the list skin (that particle, and the particles its prediction
+                                    reached that their lists lacked, walked the buckets) */
     uint64_t fast_particles;     /* variant 2: predictions that moved more than half the list skin */
     float list_skin;             /* variant 2: the list skin of the last step, units of h */
     float max_density_error_max; /* largest end-of-step max_density_error of the steps since the last reset */
